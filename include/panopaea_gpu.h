@@ -1,0 +1,245 @@
+/*
+ * panopaea_gpu.h -- C ABI of the GB300 (sm_103a) grid-fluid library.
+ *
+ * The reference (msiglreith/panopaea, Rust) exposes this path as generic
+ * traits and functions: Grid2d / Simplex1 / Simplex2 storage, the
+ * Manifold2d operators, pcg::precond_conjugate_gradient, and the advect /
+ * advect_mac / projection code of examples/dec_fluid.rs.  Every entry point
+ * below names the reference item it replaces (path:line inside the
+ * reference project).  A closure cannot cross a C ABI, so the PCG operator
+ * closure of examples/dec_fluid.rs:100-119 is built in (the masked
+ * Laplacian, scaled by dt) and the preconditioner is an enum.
+ *
+ * Conventions
+ *   - Field pointers are DEVICE pointers.  Layouts are the reference's:
+ *       cell field (Simplex2, grid.rs:76-100): row-major (y, x), h*w values;
+ *         3D: (z, y, x), d*h*w values.
+ *       face field (Simplex1, grid.rs:36-73): one buffer, part 0 = vy faces
+ *         (h+1)*w, then part 1 = vx faces h*(w+1).  3D (extension): vz faces
+ *         (d+1)*h*w, then vy d*(h+1)*w, then vx d*h*(w+1).
+ *   - All calls are asynchronous on the grid's stream (pg_grid_set_stream)
+ *     except those that return host scalars (pg_pcg_*, pg_solve_*,
+ *     pg_step_*), which synchronise that stream before returning.
+ *   - Calls on one grid handle are not thread-safe; distinct handles are.
+ *   - Every function returns a pg_status; pg_last_error() gives the
+ *     calling thread's last message.  Where the reference panics (shape
+ *     mismatch, grid too small) this ABI returns PG_BAD_ARG.
+ *   - No call falls back to the CPU: with no usable device, calls return
+ *     PG_NO_DEVICE.
+ */
+#ifndef PANOPAEA_GPU_H
+#define PANOPAEA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------- */
+/* Status codes.  The reference returns () everywhere (pcg.rs:14-82 stops    */
+/* silently after max_iterations); these make the outcomes explicit.         */
+typedef enum pg_status {
+    PG_OK = 0,
+    PG_NOT_CONVERGED = 1,  /* max_iterations reached above the threshold */
+    PG_NAN_DETECTED = 2,   /* NaN/Inf met in a CG reduction */
+    PG_TIMEOUT = 3,        /* a bounded device-side wait gave up */
+    PG_BAD_ARG = 4,        /* null pointer, bad shape, unsupported dims */
+    PG_CUDA_ERROR = 5,     /* a CUDA runtime call failed */
+    PG_NO_DEVICE = 6,      /* no CUDA device available */
+    PG_OUT_OF_MEMORY = 7,
+    PG_BREAKDOWN = 8       /* p.Ap <= 0 in CG (operator not SPD on p) */
+} pg_status;
+
+typedef enum pg_dtype { PG_F32 = 0, PG_F64 = 1 } pg_dtype;
+
+/* Field kinds, named by simplex degree as in dec/manifold.rs:19-84. */
+typedef enum pg_field_kind { PG_FACES = 1 /* Simplex1 */, PG_CELLS = 2 /* Simplex2 */ } pg_field_kind;
+
+/* Preconditioner behind pcg.rs:4-6 `trait Preconditioner`.
+ * PG_PRECOND_NONE is the reference's identity impl for () (pcg.rs:8-12);
+ * JACOBI and MG are extensions. */
+typedef enum pg_precond { PG_PRECOND_NONE = 0, PG_PRECOND_JACOBI = 1, PG_PRECOND_MG = 2 } pg_precond;
+
+typedef struct pg_grid pg_grid;
+
+/* Solve statistics (the reference prints "Iterations i", pcg.rs:61). */
+typedef struct pg_pcg_stats {
+    int64_t iterations;        /* operator applications (all rounds) */
+    int64_t refinements;       /* FP64 residual rounds (0 for plain PCG) */
+    double residual_max;       /* last ||r||inf the stop rule saw */
+    double b_max;              /* ||b||inf */
+    double threshold;          /* absolute threshold used */
+    double true_residual_max;  /* ||b - A x||inf in FP64 after the solve; -1 if not computed */
+    int32_t status;            /* pg_status of the solve */
+    int32_t reserved;
+} pg_pcg_stats;
+
+/* Pressure-solve parameters for pg_solve_pressure_* and pg_step_*. */
+typedef struct pg_solver_params {
+    int32_t precond;       /* pg_precond */
+    int32_t rel_stop;      /* 0: stop when ||r||inf < threshold (pcg.rs:58-60);
+                              1: threshold = rel_tol * ||b||inf */
+    double threshold;      /* absolute threshold (rel_stop = 0) */
+    double rel_tol;        /* relative tolerance (rel_stop = 1) */
+    int64_t max_iter;      /* max operator applications per CG run (pcg.rs:48) */
+    int32_t refine;        /* 0: one plain CG run (the reference's algorithm);
+                              n > 0: up to n FP64 residual refinement rounds */
+    int32_t check_every;   /* iterations between host convergence polls (0 = auto) */
+    double inner_rel_tol;  /* per-round relative tolerance with refine > 0 (0 = auto) */
+    int32_t mg_levels;     /* MG: number of levels (0 = auto) */
+    int32_t mg_smooth;     /* MG: red-black Gauss-Seidel sweeps pre and post (0 = 2) */
+} pg_solver_params;
+
+/* One fluid step, examples/dec_fluid.rs:46-141 (the PNG dump at :143-164
+ * is not part of the step).  Switches marked "extension" have no
+ * reference counterpart and are 0 in the reference's configuration. */
+typedef struct pg_step_params {
+    double dt;                    /* dec_fluid.rs:43 */
+    double buoyancy;              /* extension: vy += dt*buoyancy*mean(rho) on interior y faces */
+    int32_t source_enabled;       /* dec_fluid.rs:48-57 inflow box */
+    int32_t walls_after_advect;   /* extension: zero boundary faces after advection */
+    int64_t source_lo[3];         /* (z, y, x) half-open cell box; 2D uses [1],[2] */
+    int64_t source_hi[3];
+    double source_density;        /* dec_fluid.rs:53 (1.0) */
+    double source_vy;             /* dec_fluid.rs:54 (20.0) */
+    const void* source_field;     /* extension: device cell field, density = max(density, field); may be NULL */
+    int32_t zero_solid_after_project; /* extension: re-zero solid faces after projection */
+    int32_t reserved;
+    pg_solver_params solver;      /* dec_fluid.rs:91-99: pcg(&(), .., 100, threshold, ..) */
+} pg_step_params;
+
+/* ----------------------------------------------------------------------- */
+/* Errors */
+const char* pg_status_string(int status);
+const char* pg_last_error(void);
+int pg_version(void);
+
+/* ----------------------------------------------------------------------- */
+/* Grids.  Replaces Grid2d::new / Grid2d::dim (domain/grid.rs:2-15);
+ * pg_grid_create_3d defines the Grid3d the reference only declares
+ * (domain/grid.rs:17-20).  The handle also owns the solid mask, the stream
+ * and the solver workspace. */
+int pg_grid_create_2d(int64_t h, int64_t w, pg_grid** out);
+int pg_grid_create_3d(int64_t d, int64_t h, int64_t w, pg_grid** out);
+int pg_grid_destroy(pg_grid* grid);
+/* Writes (d, h, w) (d = 1 for 2D) and returns the number of dimensions (2
+ * or 3), or a negative pg_status. */
+int pg_grid_dim(const pg_grid* grid, int64_t dim_out[3]);
+/* Manifold2d::num_elem_1 / num_elem_2 (dec/grid.rs:350-356). */
+int64_t pg_grid_num_elem_1(const pg_grid* grid);
+int64_t pg_grid_num_elem_2(const pg_grid* grid);
+/* Bind a cudaStream_t (NULL = legacy default stream). */
+int pg_grid_set_stream(pg_grid* grid, void* cuda_stream);
+int pg_grid_synchronize(pg_grid* grid);
+/* Solid faces, host array in the face layout (1 = solid).  This is the
+ * obstacle masking of examples/dec_fluid.rs:71-78 and :104-112 as data:
+ * masked faces carry no flux in the RHS and no coupling in the Laplacian.
+ * NULL clears the mask. */
+int pg_grid_set_solid_faces(pg_grid* grid, const uint8_t* host_face_solid);
+/* Solid cells, host array in the cell layout (1 = solid).  Extension: a
+ * face is solid iff an adjacent cell is solid. */
+int pg_grid_set_solid_cells(pg_grid* grid, const uint8_t* host_cell_solid);
+
+/* ----------------------------------------------------------------------- */
+/* Fields.  Replaces Manifold2d::new_simplex_1 / new_simplex_2
+ * (dec/grid.rs:362-371): zero-filled device storage of the layouts above. */
+int pg_field_alloc(const pg_grid* grid, int kind, int dtype, void** dev_out);
+int pg_field_free(void* dev);
+/* Host <-> device copies, stream-ordered on the grid's stream (host
+ * memory should be pinned for overlap; pageable memory works). */
+int pg_copy_h2d(const pg_grid* grid, void* dev_dst, const void* host_src, size_t bytes);
+int pg_copy_d2h(const pg_grid* grid, void* host_dst, const void* dev_src, size_t bytes);
+
+/* ----------------------------------------------------------------------- */
+/* DEC operators (2D API parity with dec/manifold.rs:29-83).  The _f64
+ * forms take double*.  3D grids accept derivative_0_dual (negative
+ * gradient on interior faces) and mask_solid_faces; the hodge_1_* and
+ * derivative_1_primal forms are 2D-only (PG_BAD_ARG on a 3D grid). */
+
+/* hodge_1_dual (manifold.rs:74-76 -> grid.rs:223-238): primal.vy = -dual.vy, primal.vx = dual.vx */
+int pg_hodge_1_dual_f32(const pg_grid* grid, float* primal, const float* dual);
+int pg_hodge_1_dual_f64(const pg_grid* grid, double* primal, const double* dual);
+/* hodge_1_primal (manifold.rs:70-72 -> grid.rs:206-221): dual.vy = primal.vy, dual.vx = -primal.vx */
+int pg_hodge_1_primal_f32(const pg_grid* grid, float* dual, const float* primal);
+int pg_hodge_1_primal_f64(const pg_grid* grid, double* dual, const double* primal);
+/* hodge_2_primal (manifold.rs:78-80 -> grid.rs:253-255): copy */
+int pg_hodge_2_primal_f32(const pg_grid* grid, float* dual, const float* primal);
+int pg_hodge_2_primal_f64(const pg_grid* grid, double* dual, const double* primal);
+/* derivative_1_primal (manifold.rs:57-59 -> grid.rs:295-305):
+ * face = -bottom + top - left + right */
+int pg_derivative_1_primal_f32(const pg_grid* grid, float* faces, const float* edges);
+int pg_derivative_1_primal_f64(const pg_grid* grid, double* faces, const double* edges);
+/* derivative_0_dual (manifold.rs:50-52 -> grid.rs:318-334): interior faces
+ * only, boundary faces keep their value */
+int pg_derivative_0_dual_f32(const pg_grid* grid, float* edges, const float* faces);
+int pg_derivative_0_dual_f64(const pg_grid* grid, double* edges, const double* faces);
+/* Zero every solid face (examples/dec_fluid.rs:71-78, :104-112). */
+int pg_mask_solid_faces_f32(const pg_grid* grid, float* edges);
+int pg_mask_solid_faces_f64(const pg_grid* grid, double* edges);
+
+/* ----------------------------------------------------------------------- */
+/* Fused step operators. */
+
+/* The PCG operator closure of examples/dec_fluid.rs:100-119:
+ * out = dt * d1(*1^-1(M d0dual(*2 p))), i.e. dt * (-Laplacian) with solid
+ * and boundary faces closed.  One kernel; same arithmetic order. */
+int pg_laplacian_f32(const pg_grid* grid, float* out, const float* p, double dt);
+int pg_laplacian_f64(const pg_grid* grid, double* out, const double* p, double dt);
+/* The RHS of examples/dec_fluid.rs:68-83: b = -d1(*1^-1(M u)). */
+int pg_divergence_rhs_f32(const pg_grid* grid, float* b, const float* vel);
+int pg_divergence_rhs_f64(const pg_grid* grid, double* b, const double* vel);
+/* advect (examples/dec_fluid.rs:173-211): semi-Lagrangian, cell-centred,
+ * bilinear (trilinear in 3D).  Needs every dimension >= 2. */
+int pg_advect_f32(const pg_grid* grid, float* dst, const float* src, double dt, const float* vel);
+int pg_advect_f64(const pg_grid* grid, double* dst, const double* src, double dt, const double* vel);
+/* advect_mac (examples/dec_fluid.rs:213-291): MAC face advection. */
+int pg_advect_mac_f32(const pg_grid* grid, float* dst, const float* src, double dt, const float* vel);
+int pg_advect_mac_f64(const pg_grid* grid, double* dst, const double* src, double dt, const double* vel);
+/* Projection + walls (examples/dec_fluid.rs:123-141):
+ * vel += dt * d0dual(p) on interior faces, then boundary faces = 0;
+ * zero_solid != 0 (extension) also zeroes solid faces. */
+int pg_project_f32(const pg_grid* grid, float* vel, const float* p, double dt, int zero_solid);
+int pg_project_f64(const pg_grid* grid, double* vel, const double* p, double dt, int zero_solid);
+/* Wall step alone (examples/dec_fluid.rs:128-141). */
+int pg_walls_f32(const pg_grid* grid, float* vel);
+int pg_walls_f64(const pg_grid* grid, double* vel);
+
+/* ----------------------------------------------------------------------- */
+/* Solvers. */
+
+/* pcg::precond_conjugate_gradient (pcg.rs:14-82), operator = the masked
+ * Laplacian closure scaled by dt.  Same recurrence and stop rule: x = 0;
+ * return if ||b||inf < threshold; stop when ||r||inf < threshold or after
+ * max_iterations operator applications.  residual / auxiliary / search
+ * are caller-owned work vectors as in the reference (residual ends as r,
+ * auxiliary as A*p, search as p).  Reductions are accumulated in FP64. */
+int pg_pcg_f32(const pg_grid* grid, int precond, float* x, const float* b, int64_t max_iterations,
+               double threshold, float* residual, float* auxiliary, float* search, double dt,
+               pg_pcg_stats* stats);
+int pg_pcg_f64(const pg_grid* grid, int precond, double* x, const double* b, int64_t max_iterations,
+               double threshold, double* residual, double* auxiliary, double* search, double dt,
+               pg_pcg_stats* stats);
+
+/* Pressure solve A x = b with library-owned work vectors: the reference's
+ * PCG (refine = 0), or FP32 CG inside FP64 residual refinement (refine >
+ * 0), with the preconditioner of `params`.  x is overwritten (initial
+ * guess 0, as pcg.rs:32). */
+int pg_solve_pressure_f32(const pg_grid* grid, const pg_solver_params* params, float* x, const float* b,
+                          double dt, pg_pcg_stats* stats);
+
+/* One fluid step (examples/dec_fluid.rs:46-141): source -> advect density
+ * (old u) -> advect_mac u (old u) -> [walls] -> [buoyancy] -> -div ->
+ * pressure solve -> projection + walls.  vel, density, pressure are
+ * device fields updated in place; pressure receives the solution. */
+int pg_step_f32(const pg_grid* grid, const pg_step_params* params, float* vel, float* density, float* pressure,
+                pg_pcg_stats* stats);
+int pg_step_f64(const pg_grid* grid, const pg_step_params* params, double* vel, double* density,
+                double* pressure, pg_pcg_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PANOPAEA_GPU_H */

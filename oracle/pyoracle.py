@@ -1,0 +1,265 @@
+"""numpy front-end of the C++ oracle (test infrastructure only).
+
+Only the test-suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
+baseline use this module, always as the checker / the timed CPU reference;
+the product (``panopaea_gb300``) never imports it.
+
+Arrays follow the reference layouts: 2D cells (h, w), faces
+[vy (h+1)w | vx h(w+1)]; 3D cells (d, h, w), faces [vz | vy | vx].
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+
+
+class StepParams(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double),
+        ("buoyancy", C.c_double),
+        ("source_enabled", C.c_int),
+        ("source_lo", C.c_long * 3),
+        ("source_hi", C.c_long * 3),
+        ("source_density", C.c_double),
+        ("source_vy", C.c_double),
+        ("source_field", C.c_void_p),
+        ("walls_after_advect", C.c_int),
+        ("zero_solid_after_project", C.c_int),
+        ("precond", C.c_int),
+        ("rel_stop", C.c_int),
+        ("threshold", C.c_double),
+        ("rel_tol", C.c_double),
+        ("max_iter", C.c_long),
+    ]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("iterations", C.c_long), ("residual", C.c_double), ("bmax", C.c_double), ("converged", C.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build_oracle.build())
+        _lib.pgo_num_faces.restype = C.c_long
+        for s in ("f32", "f64"):
+            getattr(_lib, "pgo_pcg_" + s).restype = C.c_long
+            getattr(_lib, "pgo_norm_max_" + s).restype = C.c_double
+    return _lib
+
+
+def set_threads(n, all_loops=False):
+    lib().pgo_set_threads(int(n), int(bool(all_loops)))
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _sfx(a):
+    return {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64"}[a.dtype]
+
+
+def _shape(dims):
+    if len(dims) == 2:
+        return 2, 1, dims[0], dims[1]
+    return 3, dims[0], dims[1], dims[2]
+
+
+def num_faces(dims):
+    nd, d, h, w = _shape(dims)
+    return int(lib().pgo_num_faces(nd, C.c_long(d), C.c_long(h), C.c_long(w)))
+
+
+def _c(a):
+    assert a.flags["C_CONTIGUOUS"]
+    return a
+
+
+def hodge_1_dual(dual, dims):
+    out = np.empty_like(dual)
+    getattr(lib(), "pgo_hodge_1_dual_" + _sfx(dual))(_p(out), _p(_c(dual)), C.c_long(dims[0]), C.c_long(dims[1]))
+    return out
+
+
+def hodge_1_primal(primal, dims):
+    out = np.empty_like(primal)
+    getattr(lib(), "pgo_hodge_1_primal_" + _sfx(primal))(_p(out), _p(_c(primal)), C.c_long(dims[0]),
+                                                         C.c_long(dims[1]))
+    return out
+
+
+def derivative_1_primal(edges, dims):
+    h, w = dims
+    out = np.empty((h, w), edges.dtype)
+    getattr(lib(), "pgo_derivative_1_primal_" + _sfx(edges))(_p(out), _p(_c(edges)), C.c_long(h), C.c_long(w))
+    return out
+
+
+def derivative_0_dual(faces, dims, edges=None):
+    """grid.rs:318-334; `edges` supplies the untouched boundary values."""
+    nd, d, h, w = _shape(dims)
+    out = np.zeros(num_faces(dims), faces.dtype) if edges is None else edges.copy()
+    getattr(lib(), "pgo_derivative_0_dual_" + _sfx(faces))(_p(out), _p(_c(faces)), nd, C.c_long(d), C.c_long(h),
+                                                           C.c_long(w))
+    return out
+
+
+def mask_faces(edges, solid):
+    out = edges.copy()
+    getattr(lib(), "pgo_mask_faces_" + _sfx(edges))(_p(out), _p(_c(solid)), C.c_long(out.size))
+    return out
+
+
+def laplacian(p, dt, dims, face_solid=None):
+    nd, d, h, w = _shape(dims)
+    out = np.empty_like(p)
+    getattr(lib(), "pgo_laplacian_" + _sfx(p))(_p(out), _p(_c(p)), C.c_double(dt), _p(face_solid), nd, C.c_long(d),
+                                               C.c_long(h), C.c_long(w))
+    return out
+
+
+def divergence_rhs(vel, dims, face_solid=None):
+    nd, d, h, w = _shape(dims)
+    out = np.empty(tuple(dims), vel.dtype)
+    getattr(lib(), "pgo_divergence_rhs_" + _sfx(vel))(_p(out), _p(_c(vel)), _p(face_solid), nd, C.c_long(d),
+                                                      C.c_long(h), C.c_long(w))
+    return out
+
+
+def advect(src, dt, vel, dims):
+    nd, d, h, w = _shape(dims)
+    out = np.empty_like(src)
+    getattr(lib(), "pgo_advect_" + _sfx(src))(_p(out), _p(_c(src)), C.c_double(dt), _p(_c(vel)), nd, C.c_long(d),
+                                              C.c_long(h), C.c_long(w))
+    return out
+
+
+def advect_mac(src, dt, vel, dims):
+    nd, d, h, w = _shape(dims)
+    out = np.empty_like(src)
+    getattr(lib(), "pgo_advect_mac_" + _sfx(src))(_p(out), _p(_c(src)), C.c_double(dt), _p(_c(vel)), nd,
+                                                  C.c_long(d), C.c_long(h), C.c_long(w))
+    return out
+
+
+def project(vel, p, dt, dims, face_solid=None, zero_solid=False):
+    nd, d, h, w = _shape(dims)
+    out = vel.copy()
+    getattr(lib(), "pgo_project_" + _sfx(vel))(_p(out), _p(_c(p)), C.c_double(dt), _p(face_solid),
+                                               int(bool(zero_solid)), nd, C.c_long(d), C.c_long(h), C.c_long(w))
+    return out
+
+
+def walls(vel, dims):
+    nd, d, h, w = _shape(dims)
+    out = vel.copy()
+    getattr(lib(), "pgo_walls_" + _sfx(vel))(_p(out), nd, C.c_long(d), C.c_long(h), C.c_long(w))
+    return out
+
+
+def pcg(b, dt, dims, max_iter, threshold, precond=0, face_solid=None):
+    """pcg.rs:14-82; returns (x, r, aux, search, iterations, residual, converged)."""
+    nd, d, h, w = _shape(dims)
+    x, r, aux, s = (np.zeros_like(b) for _ in range(4))
+    res = C.c_double()
+    conv = C.c_int()
+    it = getattr(lib(), "pgo_pcg_" + _sfx(b))(int(precond), _p(x), _p(_c(b)), C.c_long(max_iter),
+                                              C.c_double(threshold), _p(r), _p(aux), _p(s), C.c_double(dt),
+                                              _p(face_solid), nd, C.c_long(d), C.c_long(h), C.c_long(w),
+                                              C.byref(res), C.byref(conv))
+    return x, r, aux, s, int(it), res.value, bool(conv.value)
+
+
+def norm_max(a):
+    return getattr(lib(), "pgo_norm_max_" + _sfx(a))(_p(_c(a)), C.c_long(a.size))
+
+
+def open_face_count(dims, face_solid=None, dtype=np.float64):
+    nd, d, h, w = _shape(dims)
+    out = np.empty(tuple(dims), dtype)
+    getattr(lib(), "pgo_open_face_count_" + _sfx(out))(_p(out), _p(face_solid), nd, C.c_long(d), C.c_long(h),
+                                                       C.c_long(w))
+    return out
+
+
+def step(vel, density, pressure, dims, params, face_solid=None):
+    """One step of examples/dec_fluid.rs:46-141 in place; returns StepStats."""
+    nd, d, h, w = _shape(dims)
+    st = StepStats()
+    getattr(lib(), "pgo_step_" + _sfx(vel))(_p(_c(vel)), _p(_c(density)), _p(_c(pressure)), _p(face_solid),
+                                            C.byref(params), C.byref(st), nd, C.c_long(d), C.c_long(h),
+                                            C.c_long(w))
+    return st
+
+
+def step_params(dt=0.05, buoyancy=0.0, source=None, source_density=1.0, source_vy=20.0, source_field=None,
+                walls_after_advect=False, zero_solid_after_project=False, precond=0, rel_stop=False,
+                threshold=0.1, rel_tol=1e-6, max_iter=100):
+    """StepParams; `source` = ((z0, y0, x0), (z1, y1, x1)) or None."""
+    p = StepParams()
+    p.dt = dt
+    p.buoyancy = buoyancy
+    p.source_enabled = int(source is not None)
+    if source is not None:
+        for i in range(3):
+            p.source_lo[i] = source[0][i]
+            p.source_hi[i] = source[1][i]
+    p.source_density = source_density
+    p.source_vy = source_vy
+    p.source_field = source_field.ctypes.data if source_field is not None else None
+    p.walls_after_advect = int(walls_after_advect)
+    p.zero_solid_after_project = int(zero_solid_after_project)
+    p.precond = precond
+    p.rel_stop = int(rel_stop)
+    p.threshold = threshold
+    p.rel_tol = rel_tol
+    p.max_iter = max_iter
+    return p
+
+
+def reference_face_mask(dims, box=((70, 80), (50, 70))):
+    """The obstacle of examples/dec_fluid.rs:71-78 as a face mask: vy[y, x]
+    and vx[y, x] are solid for y in box[0], x in box[1] (same index box in
+    both face arrays)."""
+    h, w = dims
+    m = np.zeros(num_faces(dims), np.uint8)
+    vy = m[:(h + 1) * w].reshape(h + 1, w)
+    vx = m[(h + 1) * w:].reshape(h, w + 1)
+    (y0, y1), (x0, x1) = box
+    vy[y0:y1, x0:x1] = 1
+    vx[y0:y1, x0:x1] = 1
+    return m
+
+
+def cell_mask_to_faces(cell_solid):
+    """Face is solid iff an adjacent cell is solid (the library's rule)."""
+    cs = np.asarray(cell_solid, bool)
+    if cs.ndim == 2:
+        h, w = cs.shape
+        vy = np.zeros((h + 1, w), bool)
+        vy[:-1] |= cs
+        vy[1:] |= cs
+        vx = np.zeros((h, w + 1), bool)
+        vx[:, :-1] |= cs
+        vx[:, 1:] |= cs
+        return np.concatenate([vy.ravel(), vx.ravel()]).astype(np.uint8)
+    d, h, w = cs.shape
+    vz = np.zeros((d + 1, h, w), bool)
+    vz[:-1] |= cs
+    vz[1:] |= cs
+    vy = np.zeros((d, h + 1, w), bool)
+    vy[:, :-1] |= cs
+    vy[:, 1:] |= cs
+    vx = np.zeros((d, h, w + 1), bool)
+    vx[:, :, :-1] |= cs
+    vx[:, :, 1:] |= cs
+    return np.concatenate([vz.ravel(), vy.ravel(), vx.ravel()]).astype(np.uint8)
+
+
+HAVE_LIB = os.path.exists(build_oracle.LIB)

@@ -1,0 +1,21 @@
+"""panopaea_gb300 -- the grid-fluid step of msiglreith/panopaea on GB300 (sm_103a).
+
+The compute path is ``libpanopaea_gpu.so`` (hand-written CUDA behind the C ABI
+of ``include/panopaea_gpu.h``); this package is the host-side mirror of the
+reference's Rust API (grid/field types, DEC operators, PCG, advection, step).
+"""
+
+from . import _native
+from .fluid import SolverConfig, StepConfig, advect, advect_mac, solve_pressure, step
+from .grid import Grid2d, Grid3d, Simplex1, Simplex2
+from .pcg import IDENTITY, JACOBI, LaplacianOperator, Preconditioner, precond_conjugate_gradient
+
+__all__ = [
+    "Grid2d", "Grid3d", "Simplex1", "Simplex2", "IDENTITY", "JACOBI", "LaplacianOperator", "Preconditioner",
+    "precond_conjugate_gradient", "advect", "advect_mac", "step", "solve_pressure", "StepConfig", "SolverConfig",
+]
+
+
+def load():
+    """Load (building if needed) the native library; raises if unavailable."""
+    return _native.load()

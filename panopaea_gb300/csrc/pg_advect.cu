@@ -1,0 +1,249 @@
+// pg_advect.cu -- semi-Lagrangian advection (examples/dec_fluid.rs:169-291).
+//
+// One thread per output sample.  The back-traced position, clamps, floors
+// and the lerp form of math/interp.rs:7-36 are evaluated in the reference's
+// order with non-fusing round-to-nearest arithmetic, so a float (double)
+// result equals a sequential float (double) evaluation of the Rust code.
+// 3D is an extension: trilinear (math/interp.rs:23-36) with the per-axis
+// rules of the 2D code.
+#include "pg_internal.cuh"
+
+namespace pg {
+
+constexpr int kThreads = 256;
+
+#define GRID_STRIDE(i, n) for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (i64)gridDim.x * blockDim.x)
+
+template <class T> __device__ __forceinline__ T bilerp(T a00, T a01, T a10, T a11, T s, T t) {
+    return lerp_ref(lerp_ref(a00, a01, s), lerp_ref(a10, a11, s), t);
+}
+
+// dec_fluid.rs:194-201 for one axis: p = clamp(pos - 0.5, 0, n - 1.00001);
+// i = floor(p); frac = p - i.  `hi` is n - 1.00001 rounded to T; when it
+// rounds to n-1 (float, n >= 257) the index is kept at n-2.
+template <class T> __device__ __forceinline__ void cell_coord(T pos, i64 n, T hi, i64& i0, T& frac) {
+    const T p = fmin(fmax(sub_rn(pos, T(0.5)), T(0)), hi);
+    i64 i = (i64)floor(p);
+    if (i > n - 2) i = n - 2;
+    i0 = i;
+    frac = sub_rn(p, (T)i);
+}
+
+// dec_fluid.rs:236-244 / :274-281 for one axis of a face sample.
+template <class T> __device__ __forceinline__ void face_coord(T pos, T off, i64 n, i64& i0, i64& i1, T& frac) {
+    const T q = sub_rn(pos, off);
+    const T p = fmax(floor(q), T(0));
+    const T last = (T)(n - 1);
+    i0 = (i64)fmin(p, last);
+    i1 = (i64)fmin(add_rn(p, T(1)), last);
+    frac = fmax(fmin(sub_rn(q, p), T(1)), T(0));
+}
+
+// pos + (-dt) * v  (integrate_euler, dec_fluid.rs:169-171)
+template <class T> __device__ __forceinline__ T back(T pos, T ndt, T v) { return add_rn(pos, mul_rn(ndt, v)); }
+
+// ---------------------------------------------------------------------------
+// advect, 2D (dec_fluid.rs:173-211)
+template <class T>
+__global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, i64 h, i64 w,
+                            T ndt, T hix, T hiy) {
+    const T* vy = vel;
+    const T* vx = vel + (h + 1) * w;
+    GRID_STRIDE(i, h * w) {
+        const i64 y = i / w, x = i - y * w;
+        const T vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), T(2));
+        const T vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), T(2));
+        const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
+        const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
+        i64 ix, iy;
+        T u, v;
+        cell_coord(ppx, w, hix, ix, u);
+        cell_coord(ppy, h, hiy, iy, v);
+        const T* q0 = q + iy * w + ix;
+        dst[i] = bilerp(q0[0], q0[1], q0[w], q0[w + 1], u, v);
+    }
+}
+
+// advect, 3D extension
+template <class T>
+__global__ void k_advect_3d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, Dims D, T ndt,
+                            T hix, T hiy, T hiz) {
+    const i64 h = D.h, w = D.w, hw = h * w;
+    GRID_STRIDE(i, D.nc()) {
+        const i64 zy = i / w, x = i - zy * w;
+        const i64 z = zy / h, y = zy - z * h;
+        const T vcx = div_rn(add_rn(vel[D.fx(z, y, x)], vel[D.fx(z, y, x + 1)]), T(2));
+        const T vcy = div_rn(add_rn(vel[D.fy(z, y, x)], vel[D.fy(z, y + 1, x)]), T(2));
+        const T vcz = div_rn(add_rn(vel[D.fz(z, y, x)], vel[D.fz(z + 1, y, x)]), T(2));
+        const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
+        const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
+        const T ppz = back(add_rn((T)z, T(0.5)), ndt, vcz);
+        i64 ix, iy, iz;
+        T s, t, u;
+        cell_coord(ppx, w, hix, ix, s);
+        cell_coord(ppy, h, hiy, iy, t);
+        cell_coord(ppz, D.d, hiz, iz, u);
+        const T* q0 = q + iz * hw + iy * w + ix;
+        const T* q1 = q0 + hw;
+        dst[i] = lerp_ref(bilerp(q0[0], q0[1], q0[w], q0[w + 1], s, t), bilerp(q1[0], q1[1], q1[w], q1[w + 1], s, t), u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// advect_mac, 2D (dec_fluid.rs:213-291); src/dst/vel share the face layout.
+template <class T>
+__global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, i64 h, i64 w,
+                                T ndt) {
+    const i64 n0 = (h + 1) * w, nf = n0 + h * (w + 1), wx = w + 1;
+    const T* vy = vel;
+    const T* vx = vel + n0;
+    GRID_STRIDE(i, nf) {
+        if (i >= n0) {  // x faces, qx dims (h, w+1): dec_fluid.rs:218-253
+            const i64 j = i - n0;
+            const i64 y = j / wx, x = j - y * wx;
+            const i64 xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
+            const T velx = vx[y * wx + x];
+            const T vely = div_rn(add_rn(add_rn(add_rn(vy[y * w + xc], vy[(y + 1) * w + xc]), vy[y * w + xm]),
+                                         vy[(y + 1) * w + xm]),
+                                  T(4));
+            const T ppx = back(add_rn((T)x, T(0)), ndt, velx);
+            const T ppy = back(add_rn((T)y, T(0.5)), ndt, vely);
+            i64 x0, x1, y0, y1;
+            T s, t;
+            face_coord(ppx, T(0), w + 1, x0, x1, s);
+            face_coord(ppy, T(0.5), h, y0, y1, t);
+            const T* qx = src + n0;
+            dst[i] = bilerp(qx[y0 * wx + x0], qx[y0 * wx + x1], qx[y1 * wx + x0], qx[y1 * wx + x1], s, t);
+        } else {  // y faces, qy dims (h+1, w): dec_fluid.rs:255-290
+            const i64 y = i / w, x = i - y * w;
+            const i64 yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
+            const T velx = div_rn(add_rn(add_rn(add_rn(vx[yc * wx + x], vx[yc * wx + x + 1]), vx[ym * wx + x]),
+                                         vx[ym * wx + x + 1]),
+                                  T(4));
+            const T vely = vy[y * w + x];
+            const T ppx = back(add_rn((T)x, T(0.5)), ndt, velx);
+            const T ppy = back(add_rn((T)y, T(0)), ndt, vely);
+            i64 x0, x1, y0, y1;
+            T s, t;
+            face_coord(ppx, T(0.5), w, x0, x1, s);
+            face_coord(ppy, T(0), h + 1, y0, y1, t);
+            const T* qy = src;
+            dst[i] = bilerp(qy[y0 * w + x0], qy[y0 * w + x1], qy[y1 * w + x0], qy[y1 * w + x1], s, t);
+        }
+    }
+}
+
+// Trilinear face sample of a part with dims (nz, ny, nx).
+template <class T>
+__device__ __forceinline__ T sample_part(const T* __restrict__ q, i64 nz, i64 ny, i64 nx, T ppx, T ox, T ppy, T oy,
+                                         T ppz, T oz) {
+    i64 x0, x1, y0, y1, z0, z1;
+    T s, t, u;
+    face_coord(ppx, ox, nx, x0, x1, s);
+    face_coord(ppy, oy, ny, y0, y1, t);
+    face_coord(ppz, oz, nz, z0, z1, u);
+    const T* a0 = q + z0 * ny * nx;
+    const T* a1 = q + z1 * ny * nx;
+    const T b0 = bilerp(a0[y0 * nx + x0], a0[y0 * nx + x1], a0[y1 * nx + x0], a0[y1 * nx + x1], s, t);
+    const T b1 = bilerp(a1[y0 * nx + x0], a1[y0 * nx + x1], a1[y1 * nx + x0], a1[y1 * nx + x1], s, t);
+    return lerp_ref(b0, b1, u);
+}
+
+template <class T> __device__ __forceinline__ T avg4(T a, T b, T c, T d) {
+    return div_rn(add_rn(add_rn(add_rn(a, b), c), d), T(4));
+}
+
+// advect_mac, 3D extension
+template <class T>
+__global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, Dims D,
+                                T ndt) {
+    const i64 d = D.d, h = D.h, w = D.w;
+    const i64 nz = D.nfz(), ny = D.nfy(), nf = D.nf();
+    const T* qz = src;
+    const T* qy = src + nz;
+    const T* qx = src + nz + ny;
+    GRID_STRIDE(i, nf) {
+        if (i >= nz + ny) {  // x faces (d, h, w+1)
+            const i64 j = i - nz - ny;
+            const i64 zy = j / (w + 1), x = j - zy * (w + 1);
+            const i64 z = zy / h, y = zy - z * h;
+            const i64 xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
+            const T vx_ = vel[i];
+            const T vy_ = avg4(vel[D.fy(z, y, xc)], vel[D.fy(z, y + 1, xc)], vel[D.fy(z, y, xm)], vel[D.fy(z, y + 1, xm)]);
+            const T vz_ = avg4(vel[D.fz(z, y, xc)], vel[D.fz(z + 1, y, xc)], vel[D.fz(z, y, xm)], vel[D.fz(z + 1, y, xm)]);
+            dst[i] = sample_part(qx, d, h, w + 1, back(add_rn((T)x, T(0)), ndt, vx_), T(0),
+                                 back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0.5)), ndt, vz_),
+                                 T(0.5));
+        } else if (i >= nz) {  // y faces (d, h+1, w)
+            const i64 j = i - nz;
+            const i64 zy = j / w, x = j - zy * w;
+            const i64 z = zy / (h + 1), y = zy - z * (h + 1);
+            const i64 yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
+            const T vx_ = avg4(vel[D.fx(z, yc, x)], vel[D.fx(z, yc, x + 1)], vel[D.fx(z, ym, x)], vel[D.fx(z, ym, x + 1)]);
+            const T vy_ = vel[i];
+            const T vz_ = avg4(vel[D.fz(z, yc, x)], vel[D.fz(z + 1, yc, x)], vel[D.fz(z, ym, x)], vel[D.fz(z + 1, ym, x)]);
+            dst[i] = sample_part(qy, d, h + 1, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
+                                 back(add_rn((T)y, T(0)), ndt, vy_), T(0), back(add_rn((T)z, T(0.5)), ndt, vz_), T(0.5));
+        } else {  // z faces (d+1, h, w)
+            const i64 zy = i / w, x = i - zy * w;
+            const i64 z = zy / h, y = zy - z * h;
+            const i64 zc = z < d - 1 ? z : d - 1, zm = z > 0 ? z - 1 : 0;
+            const T vx_ = avg4(vel[D.fx(zc, y, x)], vel[D.fx(zc, y, x + 1)], vel[D.fx(zm, y, x)], vel[D.fx(zm, y, x + 1)]);
+            const T vy_ = avg4(vel[D.fy(zc, y, x)], vel[D.fy(zc, y + 1, x)], vel[D.fy(zm, y, x)], vel[D.fy(zm, y + 1, x)]);
+            const T vz_ = vel[i];
+            dst[i] = sample_part(qz, d + 1, h, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
+                                 back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0)), ndt, vz_), T(0));
+        }
+    }
+}
+
+template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, double dt, const T* vel) {
+    const Dims& D = g->dims;
+    if (D.h < 2 || D.w < 2 || (D.nd == 3 && D.d < 2))
+        return bad_arg("pg_advect: every dimension must be >= 2 (the reference indexes the +1 neighbour)");
+    const T ndt = -(T)dt;
+    const T hix = (T)((double)D.w - 1.00001), hiy = (T)((double)D.h - 1.00001), hiz = (T)((double)D.d - 1.00001);
+    const int nb = grid_blocks(g, D.nc(), kThreads);
+    if (D.nd == 2)
+        k_advect_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt, hix, hiy);
+    else
+        k_advect_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt, hix, hiy, hiz);
+    PG_CHECK_LAUNCH();
+    return PG_OK;
+}
+
+template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src, double dt, const T* vel) {
+    const Dims& D = g->dims;
+    const T ndt = -(T)dt;
+    const int nb = grid_blocks(g, D.nf(), kThreads);
+    if (D.nd == 2)
+        k_advect_mac_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt);
+    else
+        k_advect_mac_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt);
+    PG_CHECK_LAUNCH();
+    return PG_OK;
+}
+
+template int launch_advect<float>(const pg_grid*, float*, const float*, double, const float*);
+template int launch_advect<double>(const pg_grid*, double*, const double*, double, const double*);
+template int launch_advect_mac<float>(const pg_grid*, float*, const float*, double, const float*);
+template int launch_advect_mac<double>(const pg_grid*, double*, const double*, double, const double*);
+
+}  // namespace pg
+
+using namespace pg;
+
+#define PG_ADV_ABI(T, SFX)                                                                               \
+    extern "C" int pg_advect_##SFX(const pg_grid* g, T* dst, const T* src, double dt, const T* vel) {   \
+        if (!g || !dst || !src || !vel) return bad_arg("pg_advect: NULL argument");                     \
+        if (dst == src) return bad_arg("pg_advect: dst must not alias src");                            \
+        return launch_advect<T>(g, dst, src, dt, vel);                                                   \
+    }                                                                                                    \
+    extern "C" int pg_advect_mac_##SFX(const pg_grid* g, T* dst, const T* src, double dt, const T* vel) { \
+        if (!g || !dst || !src || !vel) return bad_arg("pg_advect_mac: NULL argument");                 \
+        if (dst == src || dst == vel) return bad_arg("pg_advect_mac: dst must not alias src or vel");   \
+        return launch_advect_mac<T>(g, dst, src, dt, vel);                                               \
+    }
+
+PG_ADV_ABI(float, f32)
+PG_ADV_ABI(double, f64)

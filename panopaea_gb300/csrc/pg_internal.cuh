@@ -1,0 +1,159 @@
+// pg_internal.cuh -- shared definitions of the sm_103a grid-fluid library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "panopaea_gpu.h"
+
+namespace pg {
+
+typedef int64_t i64;
+
+// Face-open bits of a cell for the Laplacian (interior and not solid).
+enum : uint8_t { XLO = 1, XHI = 2, YLO = 4, YHI = 8, ZLO = 16, ZHI = 32 };
+
+// Grid shape.  2D grids are stored with d = 1 and no z faces, so the face
+// buffer is [vy (h+1)w | vx h(w+1)] exactly as dec/grid.rs:36-73; 3D grids
+// prepend the vz part.
+struct Dims {
+    int nd;
+    i64 d, h, w;
+    __host__ __device__ i64 nc() const { return d * h * w; }
+    __host__ __device__ i64 nfz() const { return nd == 3 ? (d + 1) * h * w : 0; }
+    __host__ __device__ i64 nfy() const { return d * (h + 1) * w; }
+    __host__ __device__ i64 nfx() const { return d * h * (w + 1); }
+    __host__ __device__ i64 nf() const { return nfz() + nfy() + nfx(); }
+    __host__ __device__ i64 offy() const { return nfz(); }
+    __host__ __device__ i64 offx() const { return nfz() + nfy(); }
+    __host__ __device__ i64 cell(i64 z, i64 y, i64 x) const { return (z * h + y) * w + x; }
+    __host__ __device__ i64 fz(i64 z, i64 y, i64 x) const { return (z * h + y) * w + x; }
+    __host__ __device__ i64 fy(i64 z, i64 y, i64 x) const { return offy() + (z * (h + 1) + y) * w + x; }
+    __host__ __device__ i64 fx(i64 z, i64 y, i64 x) const { return offx() + (z * h + y) * (w + 1) + x; }
+};
+
+// ---------------------------------------------------------------------------
+// Round-to-nearest arithmetic that the compiler may not fuse into FMA, so
+// the operator kernels reproduce the reference's operation order exactly.
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+// math/interp.rs:7-12: a0*(1-s) + a1*s
+template <class T> __device__ __forceinline__ T lerp_ref(T a0, T a1, T s) {
+    return add_rn(mul_rn(a0, sub_rn(T(1), s)), mul_rn(a1, s));
+}
+
+// ---------------------------------------------------------------------------
+// Block reductions in FP64 (deterministic for a fixed launch shape).
+template <int NT> __device__ __forceinline__ double block_sum(double v, double* sm) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < NT / 32) ? sm[threadIdx.x] : 0.0;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;  // valid in thread 0
+}
+
+template <int NT> __device__ __forceinline__ double block_max(double v, double* sm) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < NT / 32) ? sm[threadIdx.x] : 0.0;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident state of one CG run.  Written only by the last block of
+// each reduction kernel; read by every block at kernel entry.
+struct CgState {
+    double sigma;      // z.r of the current search direction
+    double pap;        // p.Ap
+    double alpha, beta;
+    double rmax;       // ||r||inf after the last update
+    double bmax;       // ||b||inf
+    double threshold;  // absolute stop threshold
+    double rz_new;
+    i64 iter;          // operator applications done
+    i64 max_iter;
+    int done;          // 1: stop issuing work
+    int status;        // pg_status
+    int first;         // next p-update is p = z
+    int nan_seen;
+    unsigned int counter[4];  // last-block tickets
+};
+
+// Host view of the workspace owned by a grid.
+struct Workspace {
+    double* partials = nullptr;  // per-block reduction partials (2 x kMaxBlocks)
+    CgState* state = nullptr;    // device
+    CgState* state_host = nullptr;  // pinned mirror
+    void* vec = nullptr;         // extra CG vectors (lazily sized)
+    size_t vec_bytes = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+constexpr int kMaxBlocks = 4096;
+
+}  // namespace pg
+
+struct pg_grid {
+    pg::Dims dims;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int num_sms = 0;
+    uint8_t* flags = nullptr;       // device, per cell: Laplacian face-open bits
+    uint8_t* face_solid = nullptr;  // device, per face (1 = solid) or null
+    pg::Workspace ws;
+    void* extras = nullptr;         // solver state owned by pg_solve.cu (MG levels, graphs)
+};
+
+namespace pg {
+
+// Thread-local error text.
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define PG_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return ::pg::cuda_fail(e_, #call);  \
+    } while (0)
+
+#define PG_CHECK_LAUNCH() PG_CUDA(cudaGetLastError())
+
+inline int bad_arg(const char* msg) {
+    set_error(msg);
+    return PG_BAD_ARG;
+}
+
+// Blocks for a grid-stride kernel over n items.
+inline int grid_blocks(const pg_grid* g, i64 n, int threads, int per_sm = 8) {
+    i64 b = (n + threads - 1) / threads;
+    i64 cap = (i64)g->num_sms * per_sm;
+    if (cap > kMaxBlocks) cap = kMaxBlocks;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+int ensure_workspace(pg_grid* g);
+void release_extras(pg_grid* g);
+int ensure_vec(pg_grid* g, size_t bytes);
+
+}  // namespace pg

@@ -1,0 +1,292 @@
+// pg_solve.cu -- pressure solve (plain PCG or FP64 residual refinement) and
+// the fluid step of examples/dec_fluid.rs:46-141.
+#include <algorithm>
+#include <cmath>
+
+#include "pg_cg.cuh"
+#include "pg_solve.cuh"
+
+namespace pg {
+
+// Launchers defined in pg_dec.cu / pg_advect.cu.
+template <class T> int launch_copy(const pg_grid* g, T* out, const T* in, i64 n);
+template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel);
+template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid);
+template <class T> int launch_walls(const pg_grid* g, T* vel);
+template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const pg_step_params* prm);
+template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* src);
+template <class T> int launch_buoyancy(const pg_grid* g, T* vel, const T* rho, double dt, double beta);
+template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, double dt, const T* vel);
+template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src, double dt, const T* vel);
+
+Extras* extras_of(pg_grid* g) {
+    if (!g->extras) g->extras = new Extras();
+    return (Extras*)g->extras;
+}
+
+int Extras::buffer(int slot, size_t bytes, void** out) {
+    if (bytes_[slot] < bytes) {
+        if (buf_[slot]) {
+            PG_CUDA(cudaDeviceSynchronize());
+            PG_CUDA(cudaFree(buf_[slot]));
+            buf_[slot] = nullptr;
+            bytes_[slot] = 0;
+        }
+        PG_CUDA(cudaMalloc(&buf_[slot], bytes));
+        bytes_[slot] = bytes;
+    }
+    *out = buf_[slot];
+    return PG_OK;
+}
+
+Extras::~Extras() {
+    for (int i = 0; i < kSlots; ++i) cudaFree(buf_[i]);
+    release_mg(this);
+}
+
+void release_extras(pg_grid* g) {
+    delete (Extras*)g->extras;
+    g->extras = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual r = b - A x for x held in FP64 (refinement), written as T,
+// with ||r||inf reduced to *out (device double).
+constexpr int kThreads = 256;
+
+template <int ND>
+__global__ void __launch_bounds__(kThreads)
+    k_residual64(const float* __restrict__ b, const double* __restrict__ x, const uint8_t* __restrict__ flags, Dims D,
+                 double dt, float* __restrict__ r, double* partials, unsigned int* counter, double* out) {
+    __shared__ double sm[32];
+    const i64 n = D.nc(), w = D.w, hw = D.h * D.w;
+    double m = 0.0;
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
+        const uint8_t f = flags[c];
+        const double xc = x[c];
+        double s = 0.0;
+        if (f & XLO) s += xc - x[c - 1];
+        if (f & XHI) s += xc - x[c + 1];
+        if (f & YLO) s += xc - x[c - w];
+        if (f & YHI) s += xc - x[c + w];
+        if (ND == 3) {
+            if (f & ZLO) s += xc - x[c - hw];
+            if (f & ZHI) s += xc - x[c + hw];
+        }
+        const double rv = (double)b[c] - dt * s;
+        r[c] = (float)rv;
+        m = fmax(m, fabs(rv));
+    }
+    const double bm = block_max<kThreads>(m, sm);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bm;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v = fmax(v, __ldcg(partials + i));
+    v = block_max<kThreads>(v, sm);
+    if (threadIdx.x == 0) {
+        *out = v;
+        *counter = 0;
+    }
+}
+
+__global__ void k_x64_add(double* __restrict__ x, const float* __restrict__ d, i64 n) {
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x)
+        x[c] += (double)d[c];
+}
+
+__global__ void k_x64_store(float* __restrict__ out, const double* __restrict__ x, i64 n) {
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x)
+        out[c] = (float)x[c];
+}
+
+// One FP64-residual evaluation; returns ||b - A x||inf on the host.
+static int residual64(pg_grid* g, const float* b, const double* x, double dt, float* r, double* rmax_host) {
+    Extras* ex = extras_of(g);
+    const Dims& D = g->dims;
+    const int nb = grid_blocks(g, D.nc(), kThreads, 8);
+    double* dev_out = (double*)ex->small;
+    unsigned int* counter = (unsigned int*)(dev_out + 1);
+    if (D.nd == 2)
+        k_residual64<2><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out);
+    else
+        k_residual64<3><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out);
+    PG_CHECK_LAUNCH();
+    PG_CUDA(cudaMemcpyAsync(rmax_host, dev_out, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+    PG_CUDA(cudaStreamSynchronize(g->stream));
+    return PG_OK;
+}
+
+int ensure_small(pg_grid* g) {
+    Extras* ex = extras_of(g);
+    if (!ex->small) {
+        PG_CUDA(cudaMalloc(&ex->small, 256));
+        PG_CUDA(cudaMemset(ex->small, 0, 256));
+    }
+    return PG_OK;
+}
+
+// Plain CG (the reference algorithm) with library-owned work vectors.
+template <class T>
+static int solve_plain(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, double dt, pg_pcg_stats* st) {
+    Extras* ex = extras_of(g);
+    const size_t n = (size_t)g->dims.nc();
+    void *r, *ap, *p0, *p1;
+    int rc;
+    if ((rc = ex->buffer(Extras::kR, sizeof(T) * n, &r)) || (rc = ex->buffer(Extras::kAp, sizeof(T) * n, &ap)) ||
+        (rc = ex->buffer(Extras::kP0, sizeof(T) * n, &p0)) || (rc = ex->buffer(Extras::kP1, sizeof(T) * n, &p1)))
+        return rc;
+    CgBuffers<T> buf{x, b, (T*)r, (T*)ap, {(T*)p0, (T*)p1}};
+    CgConfig cfg{prm->precond, prm->max_iter, prm->threshold, prm->rel_stop ? prm->rel_tol : 0.0, dt,
+                 prm->check_every, 1};
+    if (prm->precond == PG_PRECOND_MG) return solve_mgpcg<T>(g, prm, cfg, buf, st);
+    return run_cg<T>(g, cfg, buf, st);
+}
+
+// FP32 CG rounds inside FP64 residual refinement.
+static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, const float* b, double dt,
+                         pg_pcg_stats* st) {
+    Extras* ex = extras_of(g);
+    const i64 n = g->dims.nc();
+    int rc;
+    if ((rc = ensure_small(g))) return rc;
+    void *x64, *rr, *d, *ap, *p0, *p1;
+    if ((rc = ex->buffer(Extras::kX64, sizeof(double) * n, &x64)) || (rc = ex->buffer(Extras::kR, 4 * n, &rr)) ||
+        (rc = ex->buffer(Extras::kD, 4 * n, &d)) || (rc = ex->buffer(Extras::kAp, 4 * n, &ap)) ||
+        (rc = ex->buffer(Extras::kP0, 4 * n, &p0)) || (rc = ex->buffer(Extras::kP1, 4 * n, &p1)))
+        return rc;
+    void* rin;
+    if ((rc = ex->buffer(Extras::kRin, 4 * n, &rin))) return rc;
+    PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
+    const int nb = grid_blocks(g, n, kThreads, 8);
+    double rmax = 0.0;
+    if ((rc = residual64(g, b, (const double*)x64, dt, (float*)rin, &rmax))) return rc;
+    const double bmax = rmax;  // x = 0: r = b exactly
+    const double target = prm->rel_stop ? prm->rel_tol * bmax : prm->threshold;
+    pg_pcg_stats out{};
+    out.b_max = bmax;
+    out.threshold = target;
+    out.status = PG_NOT_CONVERGED;
+    i64 iters = 0;
+    int rounds = 0;
+    if (!(bmax < target) && !(bmax == 0.0)) {
+        for (rounds = 0; rounds < prm->refine; ++rounds) {
+            // Inner tolerance: reach half the outer target, but never ask FP32
+            // CG for more than ~1e-5 relative per round.
+            double inner = prm->inner_rel_tol > 0 ? prm->inner_rel_tol : 0.5 * target / rmax;
+            inner = std::max(inner, 1e-5);
+            CgBuffers<float> buf{(float*)d, (const float*)rin, (float*)rr, (float*)ap, {(float*)p0, (float*)p1}};
+            CgConfig cfg{prm->precond, prm->max_iter, 0.0, std::min(inner, 0.5), dt, prm->check_every, 1};
+            pg_pcg_stats s{};
+            if (prm->precond == PG_PRECOND_MG)
+                rc = solve_mgpcg<float>(g, prm, cfg, buf, &s);
+            else
+                rc = run_cg<float>(g, cfg, buf, &s);
+            if (rc) return rc;
+            iters += s.iterations;
+            if (s.status == PG_NAN_DETECTED || s.status == PG_BREAKDOWN) {
+                out.status = s.status;
+                break;
+            }
+            k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n);
+            PG_CHECK_LAUNCH();
+            if ((rc = residual64(g, b, (const double*)x64, dt, (float*)rin, &rmax))) return rc;
+            if (!std::isfinite(rmax)) {
+                out.status = PG_NAN_DETECTED;
+                break;
+            }
+            if (rmax <= target) {
+                out.status = PG_OK;
+                ++rounds;
+                break;
+            }
+            if (iters >= prm->max_iter * (i64)prm->refine) break;
+        }
+    } else {
+        out.status = PG_OK;
+    }
+    k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n);
+    PG_CHECK_LAUNCH();
+    PG_CUDA(cudaStreamSynchronize(g->stream));
+    out.iterations = iters;
+    out.refinements = rounds;
+    out.residual_max = rmax;
+    out.true_residual_max = rmax;
+    if (st) *st = out;
+    return PG_OK;
+}
+
+template <class T>
+int solve_pressure(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, double dt, pg_pcg_stats* st) {
+    if (prm->precond < PG_PRECOND_NONE || prm->precond > PG_PRECOND_MG) return bad_arg("solver: unknown precond");
+    if (prm->max_iter < 0) return bad_arg("solver: max_iter < 0");
+    if (prm->refine > 0) {
+        if (sizeof(T) != 4) return bad_arg("solver: refinement is for f32 fields");
+        return solve_refined(g, prm, (float*)x, (const float*)b, dt, st);
+    }
+    return solve_plain<T>(g, prm, x, b, dt, st);
+}
+
+// ---------------------------------------------------------------------------
+// The step (examples/dec_fluid.rs:46-141).
+template <class T>
+int step(pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure, pg_pcg_stats* st) {
+    const Dims& D = g->dims;
+    Extras* ex = extras_of(g);
+    const size_t nc = (size_t)D.nc(), nf = (size_t)D.nf();
+    void *temp, *vtemp, *b;
+    int rc;
+    if ((rc = ex->buffer(Extras::kTemp, sizeof(T) * nc, &temp)) ||
+        (rc = ex->buffer(Extras::kVelTemp, sizeof(T) * nf, &vtemp)) || (rc = ex->buffer(Extras::kB, sizeof(T) * nc, &b)))
+        return rc;
+    const double dt = prm->dt;
+    // inflow (dec_fluid.rs:48-57)
+    if (prm->source_enabled && (rc = launch_source_box<T>(g, rho, vel, prm))) return rc;
+    if (prm->source_field && (rc = launch_source_field<T>(g, rho, (const T*)prm->source_field))) return rc;
+    // advection with the old velocity (dec_fluid.rs:59-66)
+    if ((rc = launch_advect<T>(g, (T*)temp, rho, dt, vel))) return rc;
+    if ((rc = launch_advect_mac<T>(g, (T*)vtemp, vel, dt, vel))) return rc;
+    PG_CUDA(cudaMemcpyAsync(rho, temp, sizeof(T) * nc, cudaMemcpyDeviceToDevice, g->stream));
+    PG_CUDA(cudaMemcpyAsync(vel, vtemp, sizeof(T) * nf, cudaMemcpyDeviceToDevice, g->stream));
+    if (prm->walls_after_advect && (rc = launch_walls<T>(g, vel))) return rc;
+    if (prm->buoyancy != 0.0 && (rc = launch_buoyancy<T>(g, vel, rho, dt, prm->buoyancy))) return rc;
+    // -div (dec_fluid.rs:68-83)
+    if ((rc = launch_rhs<T>(g, (T*)b, vel))) return rc;
+    // pressure solve (dec_fluid.rs:87-121)
+    pg_pcg_stats s{};
+    if ((rc = solve_pressure<T>(g, &prm->solver, pressure, (const T*)b, dt, &s))) return rc;
+    // projection + walls (dec_fluid.rs:123-141)
+    if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project))) return rc;
+    PG_CUDA(cudaStreamSynchronize(g->stream));
+    if (st) *st = s;
+    return s.status;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+extern "C" int pg_solve_pressure_f32(const pg_grid* g, const pg_solver_params* prm, float* x, const float* b,
+                                     double dt, pg_pcg_stats* st) {
+    if (!g || !prm || !x || !b) return bad_arg("pg_solve_pressure: NULL argument");
+    pg_pcg_stats s{};
+    int rc = solve_pressure<float>(const_cast<pg_grid*>(g), prm, x, b, dt, &s);
+    if (rc) return rc;
+    if (st) *st = s;
+    return s.status;
+}
+
+#define PG_STEP_ABI(T, SFX)                                                                                     \
+    extern "C" int pg_step_##SFX(const pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure,     \
+                                 pg_pcg_stats* st) {                                                           \
+        if (!g || !prm || !vel || !rho || !pressure) return bad_arg("pg_step: NULL argument");                 \
+        return step<T>(const_cast<pg_grid*>(g), prm, vel, rho, pressure, st);                                  \
+    }
+
+PG_STEP_ABI(float, f32)
+PG_STEP_ABI(double, f64)

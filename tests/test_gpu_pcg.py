@@ -1,0 +1,175 @@
+"""GPU PCG (pcg.rs:14-82) against the oracle's restatement.
+
+The recurrence and stop rule are the reference's; the GPU accumulates dot
+products in FP64 (the reference sums in T, order unpinned), so iterates
+agree to rounding, not bit for bit.  Tolerances are stated per test."""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rng, seed_of
+from test_gpu_ops import cells, dev, faces, host, make_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def rhs_case(oracle, dims, seed, masked, dtype):
+    r = rng(seed)
+    nf = oracle.num_faces(dims)
+    fs = (r.random(nf) < 0.1).astype(np.uint8) if masked else None
+    vel = oracle.walls(r.standard_normal(nf), dims)
+    b = oracle.divergence_rhs(vel, dims, fs).astype(dtype)
+    return b, fs
+
+
+def run_gpu_pcg(pg, g, b, dt, max_iter, thr, precond):
+    dtype = torch.float64 if b.dtype == np.float64 else torch.float32
+    x = g.new_simplex_2(dtype)
+    rr, aux, s = g.new_simplex_2(dtype), g.new_simplex_2(dtype), g.new_simplex_2(dtype)
+    op = pg.LaplacianOperator(g, dt)
+    pre = pg.JACOBI if precond else pg.IDENTITY
+    st = pg.precond_conjugate_gradient(pre, x, pg.Simplex2(g, dev(b)), max_iter, thr, rr, aux, s, op)
+    return st, host(x), host(rr), host(aux), host(s)
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+@pytest.mark.parametrize("masked", [False, True])
+@pytest.mark.parametrize("dims", [(33, 29), (128, 128), (9, 10, 11), (32, 24, 40)])
+def test_pcg_f64_matches_oracle(pg, oracle, dims, masked, precond):
+    """f64: same iteration count (+-1) and x to 1e-9 of max|x|."""
+    b, fs = rhs_case(oracle, dims, seed_of(dims, masked), masked, np.float64)
+    g = make_grid(pg, dims)
+    if masked:
+        g.set_solid_faces(fs)
+    thr = 1e-9 * np.abs(b).max()
+    dt = 0.5
+    xo, ro, _, _, ito, reso, convo = oracle.pcg(b, dt, dims, 5000, thr, precond, fs)
+    st, x, r, aux, s = run_gpu_pcg(pg, g, b, dt, 5000, thr, precond)
+    assert convo and st["status"] == 0
+    assert abs(st["iterations"] - ito) <= 1
+    assert np.abs(x - xo).max() <= 1e-9 * np.abs(xo).max()
+    assert np.abs(r - ro).max() <= 1e-6 * np.abs(b).max()
+    # true residual
+    assert np.abs(b - oracle.laplacian(x, dt, dims, fs)).max() < 2 * thr
+
+
+@pytest.mark.parametrize("dims", [(64, 64), (16, 16, 16)])
+def test_pcg_f32_matches_oracle(pg, oracle, dims):
+    """f32 storage: iteration counts within 10%, solution to 1e-4 of max|x|."""
+    b, fs = rhs_case(oracle, dims, 7, True, np.float32)
+    g = make_grid(pg, dims)
+    g.set_solid_faces(fs)
+    thr = float(1e-5 * np.abs(b).max())
+    xo, ro, _, _, ito, reso, convo = oracle.pcg(b, 1.0, dims, 5000, thr, 0, fs)
+    st, x, r, aux, s = run_gpu_pcg(pg, g, b, 1.0, 5000, thr, 0)
+    assert convo and st["status"] == 0
+    assert abs(st["iterations"] - ito) <= max(2, 0.1 * ito)
+    assert np.abs(x - xo).max() <= 1e-4 * np.abs(xo).max()
+
+
+def test_pcg_max_iterations_tail(pg, oracle):
+    """After max_iterations the work vectors hold what pcg.rs:65-77 leaves:
+    auxiliary = M r, search = z + beta p."""
+    dims = (20, 17)
+    b, fs = rhs_case(oracle, dims, 3, False, np.float64)
+    g = make_grid(pg, dims)
+    for precond in (0, 1):
+        xo, ro, auxo, so, ito, _, convo = oracle.pcg(b, 1.0, dims, 5, 1e-300, precond)
+        st, x, r, aux, s = run_gpu_pcg(pg, g, b, 1.0, 5, 1e-300, precond)
+        assert st["iterations"] == ito == 5 and st["status"] == 1 and not convo
+        tol = 1e-10 * np.abs(b).max()
+        for got, want in ((x, xo), (r, ro), (aux, auxo), (s, so)):
+            assert np.abs(got - want).max() <= tol * max(1.0, np.abs(want).max())
+
+
+def test_pcg_converged_work_vectors(pg, oracle):
+    """On convergence: residual = r, auxiliary = A p, search = p."""
+    dims = (12, 15)
+    b, _ = rhs_case(oracle, dims, 4, False, np.float64)
+    g = make_grid(pg, dims)
+    thr = 1e-3 * np.abs(b).max()
+    xo, ro, auxo, so, ito, _, convo = oracle.pcg(b, 1.0, dims, 500, thr)
+    st, x, r, aux, s = run_gpu_pcg(pg, g, b, 1.0, 500, thr, 0)
+    assert st["iterations"] == ito and st["status"] == 0
+    for got, want in ((r, ro), (aux, auxo), (s, so)):
+        np.testing.assert_allclose(got, want, atol=1e-10 * np.abs(want).max())
+
+
+def test_pcg_early_out_and_zero_iterations(pg, oracle):
+    dims = (8, 8)
+    g = make_grid(pg, dims)
+    b = np.zeros(dims)
+    b[3, 3], b[4, 4] = 1.0, -1.0
+    st, x, *_ = run_gpu_pcg(pg, g, b, 1.0, 100, 2.0, 0)  # ||b||inf < threshold
+    assert st["iterations"] == 0 and st["status"] == 0 and np.all(x == 0)
+    st, x, *_ = run_gpu_pcg(pg, g, b, 1.0, 0, 1e-9, 0)  # no iterations allowed
+    assert st["iterations"] == 0 and st["status"] == 1 and np.all(x == 0)
+
+
+def test_pcg_nan_is_reported(pg):
+    from panopaea_gb300 import _native as N
+
+    dims = (16, 16)
+    g = make_grid(pg, dims)
+    b = np.zeros(dims, np.float32)
+    b[2, 2] = np.nan
+    b[5, 5] = 1.0
+    x, rr, aux, s = (g.new_simplex_2() for _ in range(4))
+    with pytest.raises(N.PgError) as ei:
+        pg.precond_conjugate_gradient(pg.IDENTITY, x, pg.Simplex2(g, dev(b)), 50, 1e-6, rr, aux, s,
+                                      pg.LaplacianOperator(g, 1.0))
+    assert ei.value.status == N.PG_NAN_DETECTED
+
+
+def test_pcg_rejects_host_closure(pg):
+    g = make_grid(pg, (4, 4))
+    x = g.new_simplex_2()
+    with pytest.raises(TypeError):
+        pg.precond_conjugate_gradient((), x, x, 10, 0.1, x, x, x, lambda out, p: None)
+
+
+@pytest.mark.parametrize("dims,precond", [((256, 256), 0), ((96, 96, 96), 1), ((128, 128, 128), 0)])
+def test_solve_full_size_properties(pg, oracle, dims, precond):
+    """Larger sizes, checked by size-independent properties: the solver's
+    own stop rule holds, the FP64 true residual of the returned x is small,
+    and the projected field is divergence-free to that residual."""
+    r = rng(seed_of(dims))
+    nf = oracle.num_faces(dims)
+    vel = oracle.walls(r.standard_normal(nf).astype(np.float32), dims)
+    g = make_grid(pg, dims)
+    v = faces(pg, g, vel)
+    b = g.new_simplex_2()
+    g.divergence_rhs(b, v)
+    x = g.new_simplex_2()
+    tol = 1e-5
+    st = pg.solve_pressure(g, x, b, 0.5, pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=tol,
+                                                         max_iter=20000))
+    assert st["status"] == 0
+    bh = host(b).astype(np.float64)
+    xh = host(x).astype(np.float64)
+    true_r = np.abs(bh - oracle.laplacian(xh, 0.5, dims)).max()
+    assert true_r <= 20 * tol * np.abs(bh).max()
+    g.project(v, x, 0.5)
+    div = oracle.divergence_rhs(host(v).astype(np.float64), dims)
+    assert np.abs(div).max() <= 20 * tol * np.abs(bh).max()
+
+
+@pytest.mark.parametrize("dims", [(128, 128), (64, 64, 64)])
+def test_refined_solve_reaches_fp64_tolerance(pg, oracle, dims):
+    """FP32 CG inside FP64 residual refinement reaches a true relative
+    residual of 1e-6 (checked in FP64 by the oracle's operator)."""
+    r = rng(seed_of(dims, "ref"))
+    nf = oracle.num_faces(dims)
+    vel = oracle.walls(r.standard_normal(nf).astype(np.float32), dims)
+    g = make_grid(pg, dims)
+    b = g.new_simplex_2()
+    g.divergence_rhs(b, faces(pg, g, vel))
+    x = g.new_simplex_2()
+    st = pg.solve_pressure(g, x, b, 0.5, pg.SolverConfig(rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4))
+    assert st["status"] == 0 and st["refinements"] >= 1
+    bh = host(b).astype(np.float64)
+    true_r = np.abs(bh - oracle.laplacian(host(x).astype(np.float64), 0.5, dims)).max()
+    # x is returned in FP32: allow its rounding on top of the FP64 target
+    assert st["true_residual_max"] <= 1e-6 * np.abs(bh).max()
+    assert true_r <= 1e-5 * np.abs(bh).max()
