@@ -1,0 +1,459 @@
+#!/usr/bin/env python
+"""Throughput of the grid-fluid step on GB300, in Mcell-steps/s.
+
+Default workload: the 3D precision study -- a 256^3 MAC grid, f32 fields,
+filtered-noise velocity (max |u| = 2 cells/step, dt = 1), solid walls; a
+step is trilinear advection of velocity and density, the 7-point pressure
+projection to relative residual 1e-6, and the gradient subtraction.  Each
+step continues the simulation from the previous one.
+
+Two solver forms run on the same workload:
+  chosen -- multigrid-preconditioned CG (falls back to Jacobi-PCG when the
+            library has no MG) inside FP64 residual refinement;
+  plain  -- the reference's unpreconditioned CG in FP32 storage.
+`value` is the chosen form; the plain form is reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU (torchrun, one rank per GPU): every rank advances its own replica
+grid (the step has no data-path exchange), `value` = all cells x steps over
+the max time over ranks ("scaling": "weak").
+
+--impl reference times the reference's CPU algorithm (the oracle restatement,
+the reference's threading: derivative_0_dual / derivative_1_primal parallel,
+everything else serial) on the host cores, on a bounded sample per step.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s at rel. residual 1e-6 on 1 GB300; chosen form vs plain FP32 PCG"
+UNIT = "Mcell-steps/s"
+
+# Algorithmic bytes per cell for one launch of each kernel kind (f32 fields,
+# uint8 face-open flags), 3D / 2D.  See the design doc for the derivations.
+BYTES_PER_CELL = {
+    "cg_spmv": (17, 17),        # r, p_old, flags in; p_new, Ap out
+    "cg_update": (24, 24),      # x, p, r, Ap in; x, r out (Jacobi: +1 flags)
+    "cg_init": (13, 13),        # b in; x, r out; flags (Jacobi)
+    "advect": (20, 16),         # rho + 3 (2) faces in, rho out
+    "advect_mac": (24, 16),     # 3 (2) faces in (self-advection), 3 (2) out
+    "rhs": (17, 13),            # faces + flags in, b out
+    "project": (29, 21),        # p, faces, flags in; faces out
+    "residual64": (17, 17),     # b, x64, flags in; r out
+    "refine_update": (20, 20),  # x64, d in; x64 out
+    # fine-level multigrid kernels, per fine cell:
+    "mg_smooth": (6.5, 6.5),    # half-sweep: f, flags of its colour, e of the other in; e of its colour out
+    "mg_restrict": (9.5, 9.5),  # e, f, flags in; coarse f (1/8 or 1/4 of the cells) out
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="precision_3d_256")
+    ap.add_argument("--dims", default=None, help="override, e.g. 128,128,128")
+    ap.add_argument("--plain-steps", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-PCG comparison (profiling runs)")
+    ap.add_argument("--cpu-cap", type=int, default=16, help="CG iterations per CPU sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas; only the barrier and the max over ranks)
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, ws, rank, local, backend):
+        import torch
+
+        self.ws, self.rank, self.local = ws, rank, local
+        self.torch = torch
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            if self.torch.cuda.is_available():
+                self.pg.barrier(device_ids=[self.local])
+            else:
+                self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        dev = "cuda" if self.torch.cuda.is_available() else "cpu"
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for ln in open(self.path):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(f[1]), smax=float(f[2]), power=float(f[3]), hw=f[5], hwt=f[6], swt=f[7],
+                                 pcap=f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        pmax = max(r["power"] for r in rows)
+        load = [r for r in rows if r["power"] >= 0.5 * pmax] or rows
+        reasons = set()
+        for r in rows:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                              ("pcap", "sw_power_cap")):
+                if r[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in load), "sm_max_mhz": max(r["smax"] for r in rows),
+                "power_w_max": pmax, "samples": len(rows), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kind, workload):
+    """Per-launch DRAM bytes of `kind` from the committed ncu summary, if any
+    (lines `traffic <kind> <workload> <bytes_per_launch>`)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        f = ln.split()
+        if len(f) >= 4 and f[0] == "traffic" and f[1] == kind and f[2] == workload:
+            return float(f[3])
+    return None
+
+
+def solver_cfgs(pg, rel_tol, have_mg):
+    chosen = pg.SolverConfig(precond=2 if have_mg else 1, rel_stop=True, rel_tol=rel_tol, max_iter=20000, refine=4)
+    plain = pg.SolverConfig(precond=0, rel_stop=True, rel_tol=rel_tol, max_iter=200000)
+    return chosen, plain
+
+
+def step_cfg(pg, spec, solver):
+    return pg.StepConfig(dt=spec["dt"], buoyancy=spec["buoyancy"], source_enabled=False, walls_after_advect=True,
+                         zero_solid_after_project=True, solver=solver)
+
+
+def have_mg(pg, grid):
+    """Probe the MG preconditioner on a tiny problem."""
+    import torch
+
+    g = pg.Grid3d((8, 8, 8)) if grid.ndim == 3 else pg.Grid2d((8, 8))
+    b = g.new_simplex_2()
+    b.data.view(-1)[0], b.data.view(-1)[-1] = 1.0, -1.0
+    x = g.new_simplex_2()
+    try:
+        st = pg.solve_pressure(g, x, b, 1.0, pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=100))
+        torch.cuda.synchronize()
+        return st["status"] == 0
+    except Exception:
+        return False
+
+
+# ---------------------------------------------------------------------------
+# CPU: the reference algorithm on the host cores (oracle restatement)
+
+def cpu_sample(O, dims, spec, vel0, rho0, cap, n_full=None):
+    """One step of the reference algorithm on the host: advection, RHS and
+    projection in full, the CG truncated at `cap` iterations and its time
+    scaled to the `n_full` iterations the same CG needs to converge (n_full
+    measured untimed with every loop parallel when not given)."""
+    threads = os.cpu_count() or 1
+    dt = spec["dt"]
+    O.set_threads(threads, all_loops=False)  # the reference's threading
+    vel = vel0.astype(np.float32).copy()
+    rho = rho0.astype(np.float32).copy()
+    t0 = time.perf_counter()
+    rho_n = O.advect(rho, dt, vel, dims)
+    vel_n = O.advect_mac(vel, dt, vel, dims)
+    vel_n = O.walls(vel_n, dims)
+    b = O.divergence_rhs(vel_n, dims)
+    t1 = time.perf_counter()
+    thr = spec["rel_tol"] * float(np.abs(b).max())
+    tc0 = time.perf_counter()
+    x, _, _, _, it, res, conv = O.pcg(b, dt, dims, cap, thr)
+    tc1 = time.perf_counter()
+    t2 = time.perf_counter()
+    O.project(vel_n, x, dt, dims)
+    t3 = time.perf_counter()
+    t_fixed = (t1 - t0) + (t3 - t2)
+    t_iter = (tc1 - tc0) / max(it, 1)
+    if n_full is None:
+        O.set_threads(threads, all_loops=True)
+        n_full = O.pcg(b, dt, dims, 1000000, thr)[4]
+        O.set_threads(threads, all_loops=False)
+    t_step = t_fixed + n_full * t_iter
+    cells = int(np.prod(dims))
+    return {"value": cells / t_step / 1e6, "t_step_s": t_step, "t_fixed_s": t_fixed, "t_iter_s": t_iter,
+            "n_full": int(n_full), "cap": int(it), "threads": threads, "wall_s": t3 - t0}
+
+
+def reference_arm(args, spec, dims):
+    ws, rank, local = dist_setup()
+    if rank != 0:
+        return
+    from oracle import pyoracle as O
+    from panopaea_gb300 import workloads as W
+
+    vel0, rho0 = W.initial_state(args.workload, dims)
+    n_full = None
+    vals = []
+    for i in range(args.warmup + args.steps):
+        s = cpu_sample(O, dims, spec, vel0, rho0, args.cpu_cap, n_full)
+        n_full = s["n_full"]
+        if i >= args.warmup:
+            vals.append(s)
+    value = statistics.median(v["value"] for v in vals)
+    sample = ("one %s step per bench step: advection, RHS, projection in full, CG truncated at %d iterations, "
+              "time scaled to the %d iterations the reference CG needs (measured untimed)" %
+              ("x".join(map(str, dims)), vals[0]["cap"], n_full))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(v["t_step_s"] for v in vals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "dims": list(dims), "form": "reference CG (identity preconditioner)",
+                   "threading": "reference (rayon loops parallel, rest serial)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": vals[0]["threads"], "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+
+def timed_steps(torch, pg, dist, grid, cfg, gv, gr, gp, k):
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(k):
+        stats.append(pg.step(grid, cfg, gv, gr, gp))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    return e0.elapsed_time(e1), stats
+
+
+def ours(args, spec, dims):
+    import torch
+
+    import panopaea_gb300 as pg
+    from panopaea_gb300 import _native as N
+    from panopaea_gb300 import workloads as W
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = Dist(ws, rank, local, "nccl")
+    lib = pg.load()
+    cells = int(np.prod(dims))
+    vel0, rho0 = W.initial_state(args.workload, dims)
+    grid = pg.Grid3d(dims) if len(dims) == 3 else pg.Grid2d(dims)
+    mg = have_mg(pg, grid)
+    chosen, plain = solver_cfgs(pg, spec["rel_tol"], mg)
+    cfg_c, cfg_p = step_cfg(pg, spec, chosen), step_cfg(pg, spec, plain)
+
+    def fresh():
+        return (pg.Simplex1(grid, torch.from_numpy(vel0).cuda()), pg.Simplex2(grid, torch.from_numpy(rho0).cuda()),
+                grid.new_simplex_2())
+
+    # --- chosen form: warm-up, then the timed region (profiled) ------------
+    gv, gr, gp = fresh()
+    for _ in range(args.warmup):
+        pg.step(grid, cfg_c, gv, gr, gp)
+    torch.cuda.synchronize()
+    lib.pg_profile_reset()
+    lib.pg_profile_enable(1)
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = lib.pg_kernel_launches()
+    ms, stats = timed_steps(torch, pg, dist, grid, cfg_c, gv, gr, gp, args.steps)
+    launches = lib.pg_kernel_launches() - launches0
+    clk = clocks.stop()
+    lib.pg_profile_enable(0)
+    ms_max = dist.max(ms)
+    value = ws * cells * args.steps / (ms_max / 1e3) / 1e6
+    kinds = {}
+    import ctypes as C
+
+    for k in range(lib.pg_profile_num_kinds()):
+        t = C.c_double()
+        n = C.c_int64()
+        lib.pg_profile_read(k, C.byref(t), C.byref(n))
+        if n.value:
+            kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
+    its = [s["iterations"] for s in stats]
+    # --- plain FP32 PCG on the same workload -------------------------------
+    plain_out = None
+    if not args.no_plain:
+        gv2, gr2, gp2 = fresh()
+        pg.step(grid, cfg_p, gv2, gr2, gp2)  # warm-up
+        kp = args.plain_steps or max(1, min(args.steps, 3))
+        ms_p, st_p = timed_steps(torch, pg, dist, grid, cfg_p, gv2, gr2, gp2, kp)
+        ms_p = dist.max(ms_p)
+        value_plain = ws * cells * kp / (ms_p / 1e3) / 1e6
+        plain_out = {"value": value_plain, "unit": UNIT, "ms_per_step": ms_p / kp,
+                     "iterations_per_step": [s["iterations"] for s in st_p], "speedup_of_chosen": value / value_plain}
+        del gv2, gr2, gp2
+    # --- e2e through the public API with host buffers ---------------------
+    e2e = None
+    if not args.no_e2e:
+        hv = torch.from_numpy(vel0.copy()).pin_memory()
+        hr = torch.from_numpy(rho0.copy()).pin_memory()
+        stream = torch.cuda.current_stream()
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            gv.data.copy_(hv, non_blocking=True)
+            gr.data.copy_(hr, non_blocking=True)
+            pg.step(grid, cfg_c, gv, gr, gp)
+            hv.copy_(gv.data, non_blocking=True)
+            hr.copy_(gr.data, non_blocking=True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms_e = dist.max(t0.elapsed_time(t1))
+        nb = (vel0.size + rho0.size) * 4
+        e2e = {"value": ws * cells * args.steps / (ms_e / 1e3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": nb,
+               "d2h_bytes_per_step": nb, "ms_per_step": ms_e / args.steps}
+    # --- roofline of the dominant kernel ------------------------------------
+    peak, peak_src = peaks()
+    dom = max(kinds, key=lambda k: kinds[k][0]) if kinds else None
+    roof = None
+    if dom:
+        tot, n = kinds[dom]
+        bpc = BYTES_PER_CELL.get(dom, (0, 0))[0 if len(dims) == 3 else 1]
+        per_launch_ms = tot / n
+        achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": ncu_traffic(dom, args.workload),
+                "algorithmic_bytes_per_launch": bpc * cells, "avg_launch_ms": per_launch_ms, "launches": n,
+                "share_of_timed": tot / ms}
+    # --- CPU baseline (rank 0, N = 1) ---------------------------------------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle import pyoracle as O
+
+        s = cpu_sample(O, dims, spec, vel0, rho0, args.cpu_cap)
+        cpu = {"value": s["value"], "unit": UNIT, "cores": s["threads"], "kind": "port",
+               "sample": "one %s step: advection, RHS, projection in full (reference threading), CG truncated at %d "
+                         "iterations and scaled to the %d the reference CG needs (counted untimed, all loops "
+                         "parallel); %.1f s of CPU wall time" % ("x".join(map(str, dims)), s["cap"], s["n_full"],
+                                                                 s["wall_s"])}
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "dims": list(dims), "cells": cells, "dt": spec["dt"],
+                       "rel_tol": spec["rel_tol"],
+                       "form": ("MG-preconditioned CG" if mg else "Jacobi-PCG") + " in FP64 residual refinement",
+                       "parallelism": "replicas x%d" % ws,
+                       "l2": "inputs larger than L2 (%.0f MB of fields per step)" % ((vel0.size + rho0.size * 3) * 4 / 1e6)},
+            "iterations_per_step": its,
+            "true_residual_rel": [s["true_residual_max"] / s["b_max"] if s["b_max"] else 0.0 for s in stats],
+            "plain_fp32_pcg": plain_out,
+            "roofline": roof,
+            "kernels_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in sorted(kinds.items(), key=lambda kv: -kv[1][0])},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
+        }
+        print(json.dumps(out), flush=True)
+    dist.close()
+
+
+def main():
+    args = parse_args()
+    from panopaea_gb300 import workloads as W
+
+    spec = W.WORKLOADS[args.workload]
+    dims = tuple(int(v) for v in args.dims.split(",")) if args.dims else tuple(spec["dims"])
+    if args.impl == "reference":
+        reference_arm(args, spec, dims)
+    else:
+        ours(args, spec, dims)
+
+
+if __name__ == "__main__":
+    main()

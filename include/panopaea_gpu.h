@@ -238,6 +238,21 @@ int pg_step_f32(const pg_grid* grid, const pg_step_params* params, float* vel, f
 int pg_step_f64(const pg_grid* grid, const pg_step_params* params, double* vel, double* density,
                 double* pressure, pg_pcg_stats* stats);
 
+/* ----------------------------------------------------------------------- */
+/* Instrumentation (no reference counterpart; the reference only prints
+ * wall-clock ms around the PCG, examples/dec_fluid.rs:87,121). */
+
+/* Kernel launches issued by this library since it was loaded. */
+int64_t pg_kernel_launches(void);
+/* on != 0: record a CUDA event pair around every launch, per kernel kind. */
+int pg_profile_enable(int on);
+int pg_profile_reset(void);
+int pg_profile_num_kinds(void);
+const char* pg_profile_kind_name(int kind);
+/* Waits for the recorded events and returns the summed device time (ms)
+ * and launch count of one kernel kind. */
+int pg_profile_read(int kind, double* total_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,7 @@
 // or parallelises every loop (all=1, used only to make tests faster).
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
@@ -42,6 +43,7 @@ namespace {
 
 int g_threads = 1;
 int g_all = 0;
+int g_dot64 = 0;  // 1: accumulate dot products in double (the GPU's choice)
 
 #define PGO_STR(x) #x
 #define PGO_PRAGMA(x) _Pragma(PGO_STR(x))
@@ -419,6 +421,11 @@ template <class T> T norm_max(const T* a, idx n) {
 // math/linear_view.rs:12-14 (ndarray 1-D dot; summation order of ndarray 0.10
 // is not pinned: a serial sum in T is used).
 template <class T> T dot(const T* a, const T* b, idx n) {
+    if (g_dot64) {
+        double s = 0.0;
+        for (idx i = 0; i < n; ++i) s += (double)a[i] * (double)b[i];
+        return (T)s;
+    }
     T s = T(0);
     for (idx i = 0; i < n; ++i) s = s + a[i] * b[i];
     return s;
@@ -587,6 +594,7 @@ struct pgo_step_stats {
     long iterations;
     double residual, bmax;
     int converged;
+    double t_total, t_solve;  // wall seconds: whole step, and the pcg call
 };
 
 namespace {
@@ -620,6 +628,7 @@ inline idx vy_face_index(const Shape& s, idx z, idx y, idx x) {
 template <class T>
 void step(const Shape& s, T* vel, T* density, T* pressure, const uint8_t* fs, const pgo_step_params& prm,
           pgo_step_stats* st) {
+    const auto t0 = std::chrono::steady_clock::now();
     const idx nc = s.nc(), nf = s.nf();
     const T dt = (T)prm.dt;
     // inflow
@@ -660,10 +669,15 @@ void step(const Shape& s, T* vel, T* density, T* pressure, const uint8_t* fs, co
     if (prm.rel_stop) thr = (T)(prm.rel_tol * (double)norm_max(b.data(), nc));
     T res;
     int conv;
+    const auto t1 = std::chrono::steady_clock::now();
     long it = pcg(prm.precond, pressure, b.data(), prm.max_iter, thr, r.data(), aux.data(), search.data(), dt, fs, s,
                   &res, &conv);
+    const auto t2 = std::chrono::steady_clock::now();
     project(vel, pressure, dt, fs, prm.zero_solid_after_project, s);
+    const auto t3 = std::chrono::steady_clock::now();
     if (st) {
+        st->t_total = std::chrono::duration<double>(t3 - t0).count();
+        st->t_solve = std::chrono::duration<double>(t2 - t1).count();
         st->iterations = it;
         st->residual = (double)res;
         st->bmax = (double)norm_max(b.data(), nc);
@@ -682,6 +696,9 @@ PGO_EXPORT void pgo_set_threads(int n, int all) {
     g_threads = n < 1 ? 1 : n;
     g_all = all;
 }
+
+// 1: dot products accumulate in double (as the CUDA library does); 0: in T.
+PGO_EXPORT void pgo_set_dot64(int on) { g_dot64 = on; }
 
 PGO_EXPORT long pgo_num_faces(int nd, long d, long h, long w) { return shape_of(nd, d, h, w).nf(); }
 

@@ -39,7 +39,8 @@ class StepParams(C.Structure):
 
 
 class StepStats(C.Structure):
-    _fields_ = [("iterations", C.c_long), ("residual", C.c_double), ("bmax", C.c_double), ("converged", C.c_int)]
+    _fields_ = [("iterations", C.c_long), ("residual", C.c_double), ("bmax", C.c_double), ("converged", C.c_int),
+                ("t_total", C.c_double), ("t_solve", C.c_double)]
 
 
 def lib():
@@ -55,6 +56,12 @@ def lib():
 
 def set_threads(n, all_loops=False):
     lib().pgo_set_threads(int(n), int(bool(all_loops)))
+
+
+def set_dot64(on):
+    """Accumulate dot products in double (the library's choice) or in T
+    (the reference's ndarray dot, the default)."""
+    lib().pgo_set_dot64(int(bool(on)))
 
 
 def _p(a):

@@ -110,6 +110,12 @@ _SIGS = {
     "pg_copy_h2d": (_I, [_P, _P, _P, C.c_size_t]),
     "pg_copy_d2h": (_I, [_P, _P, _P, C.c_size_t]),
     "pg_solve_pressure_f32": (_I, [_P, C.POINTER(SolverParams), _P, _P, _D, C.POINTER(PcgStats)]),
+    "pg_kernel_launches": (_I64, []),
+    "pg_profile_enable": (_I, [_I]),
+    "pg_profile_reset": (_I, []),
+    "pg_profile_num_kinds": (_I, []),
+    "pg_profile_kind_name": (C.c_char_p, [_I]),
+    "pg_profile_read": (_I, [_I, C.POINTER(_D), C.POINTER(_I64)]),
 }
 for _sfx in ("f32", "f64"):
     _SIGS.update({

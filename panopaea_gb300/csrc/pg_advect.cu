@@ -36,7 +36,11 @@ template <class T> __device__ __forceinline__ void face_coord(T pos, T off, i64 
     const T last = (T)(n - 1);
     i0 = (i64)fmin(p, last);
     i1 = (i64)fmin(add_rn(p, T(1)), last);
-    frac = fmax(fmin(sub_rn(q, p), T(1)), T(0));
+    // .min(1.0).max(0.0) with Rust's NaN rule: NaN.min(1) = 1.  Written out
+    // because the compiler turns fmax(fmin(v, 1), 0) into a saturate, which
+    // maps NaN to 0.
+    const T v = sub_rn(q, p);
+    frac = (v != v) ? T(1) : fmax(fmin(v, T(1)), T(0));
 }
 
 // pos + (-dt) * v  (integrate_euler, dec_fluid.rs:169-171)
@@ -205,9 +209,9 @@ template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, dou
     const T hix = (T)((double)D.w - 1.00001), hiy = (T)((double)D.h - 1.00001), hiz = (T)((double)D.d - 1.00001);
     const int nb = grid_blocks(g, D.nc(), kThreads);
     if (D.nd == 2)
-        k_advect_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt, hix, hiy);
+        PG_LAUNCH(KK_ADVECT, g->stream, k_advect_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt, hix, hiy));
     else
-        k_advect_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt, hix, hiy, hiz);
+        PG_LAUNCH(KK_ADVECT, g->stream, k_advect_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt, hix, hiy, hiz));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -217,9 +221,9 @@ template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src,
     const T ndt = -(T)dt;
     const int nb = grid_blocks(g, D.nf(), kThreads);
     if (D.nd == 2)
-        k_advect_mac_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt);
+        PG_LAUNCH(KK_ADVECT_MAC, g->stream, k_advect_mac_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt));
     else
-        k_advect_mac_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt);
+        PG_LAUNCH(KK_ADVECT_MAC, g->stream, k_advect_mac_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }

@@ -1,14 +1,20 @@
 // pg_cg.cu -- conjugate gradient on the masked Laplacian (pcg.rs:14-82).
 //
 // Per iteration two kernels, each one pass over HBM:
-//   k_cg_spmv   p = z + beta*p (z = M r recomputed on the fly, p = z on the
-//               first iteration), Ap = A p with the neighbours' new p
-//               recomputed from r and the old p, and p.Ap in FP64;
-//   k_cg_update x += alpha p, r -= alpha Ap, ||r||inf and z.r in FP64.
+//   k_cg_spmv   p = z + beta*p (p = z on the first iteration), Ap = A p with
+//               the neighbours' new p recomputed from their inputs, p.Ap;
+//   k_cg_update x += alpha p, r -= alpha Ap, ||r||inf and z.r.
+// z = M^-1 r is r (identity, pcg.rs:8-12), r / diag (Jacobi, on the fly from
+// the face-open bits) or read from a buffer an outer preconditioner wrote
+// (multigrid, which then also reduces z.r).
 // The scalars (sigma, alpha, beta, the stop test) live in a device-side
 // CgState written by the last block of each reduction kernel, so the host
-// only polls a pinned copy every few iterations and never sits between two
-// kernels.  Once the stop test fires every later kernel returns at entry.
+// polls a pinned copy every few iterations and never sits between kernels.
+// Once the stop test fires every later kernel returns at entry.
+//
+// GB300 runs FP64 at 1/64 of the FP32 rate, so no per-cell work is FP64:
+// each thread accumulates a compensated FP32 partial (float fields) and
+// only the cross-thread and cross-block reduction tree is FP64.
 #include <algorithm>
 
 #include "pg_cg.cuh"
@@ -17,64 +23,57 @@ namespace pg {
 
 constexpr int kCgThreads = 256;
 
-template <class T, int PRE> __device__ __forceinline__ T precond_apply(T r, uint8_t f, T dt) {
-    if (PRE == PG_PRECOND_JACOBI) {
-        const int n = __popc((unsigned)f);
-        return n ? div_rn(r, mul_rn((T)n, dt)) : T(0);
+template <class T> __device__ __forceinline__ T rcp_rn(T v);
+template <> __device__ __forceinline__ float rcp_rn<float>(float v) { return __frcp_rn(v); }
+template <> __device__ __forceinline__ double rcp_rn<double>(double v) { return __drcp_rn(v); }
+
+// z = M^-1 r at one cell for PM_NONE / PM_JACOBI.
+template <class T, int PM> __device__ __forceinline__ T zval(const T* __restrict__ r, const uint8_t* __restrict__ flags,
+                                                             const T* __restrict__ zb, i64 k, T dt) {
+    if (PM == PM_JACOBI) {
+        const int n = __popc((unsigned)flags[k]);
+        return n ? r[k] * rcp_rn<T>((T)n * dt) : T(0);
     }
-    return r;
+    if (PM == PM_ZBUF) return zb[k];
+    return r[k];
 }
 
-// Last-block ticket: returns true in every thread of the block that
-// finished last.  Partial sums must be written (by thread 0) before.
-__device__ __forceinline__ bool last_block(unsigned int* counter) {
-    __shared__ bool am_last;
-    __threadfence();
-    if (threadIdx.x == 0) {
-        const unsigned int t = atomicAdd(counter, 1u);
-        am_last = (t == gridDim.x - 1);
+// z for a value already in a register (PM_NONE / PM_JACOBI).
+template <class T, int PM> __device__ __forceinline__ T zof(T rv, const uint8_t* __restrict__ flags, i64 k, T dt) {
+    if (PM == PM_JACOBI) {
+        const int n = __popc((unsigned)flags[k]);
+        return n ? rv * rcp_rn<T>((T)n * dt) : T(0);
     }
-    __syncthreads();
-    return am_last;
+    return rv;
 }
 
-// Deterministic sum (or max) of n partials by one block.
-template <bool MAX> __device__ double reduce_partials(const double* partials, int n, double* sm) {
-    double v = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double pv = __ldcg(partials + i);
-        v = MAX ? fmax(v, pv) : v + pv;
-    }
-    return MAX ? block_max<kCgThreads>(v, sm) : block_sum<kCgThreads>(v, sm);
-}
-
-template <class T, int PRE>
+template <class T, int PM>
 __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ b,
                                                           const uint8_t* __restrict__ flags, i64 n, T dt, double thr,
                                                           double rel_tol, i64 max_iter, int zero_x, CgState* st,
                                                           double* partials) {
     __shared__ double sm[32];
-    double bm = 0.0, sig = 0.0;
+    Acc<T> sig;
+    T bm = T(0);
     int bad = 0;
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
         const T bv = b[c];
         if (zero_x) x[c] = T(0);
         r[c] = bv;
-        const T z = precond_apply<T, PRE>(bv, PRE ? flags[c] : 0, dt);
-        bm = fmax(bm, fabs((double)bv));
-        sig += (double)z * (double)bv;
+        bm = fmax(bm, fabs(bv));
         bad |= !isfinite(bv);
+        if (PM != PM_ZBUF) sig.add(zof<T, PM>(bv, flags, c, dt) * bv);
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
-    const double bsum = block_max<kCgThreads>(bm, sm);
-    const double ssum = block_sum<kCgThreads>(sig, sm);
+    const double bsum = block_max<kCgThreads>((double)bm, sm);
+    const double ssum = block_sum<kCgThreads>(sig.value(), sm);
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = bsum;
-        partials[gridDim.x + blockIdx.x] = ssum;
+        partials[kMaxBlocks + blockIdx.x] = ssum;
     }
     if (!last_block(&st->counter[0])) return;
-    const double bmax = reduce_partials<true>(partials, gridDim.x, sm);
-    const double sigma = reduce_partials<false>(partials + gridDim.x, gridDim.x, sm);
+    const double bmax = reduce_partials<true, kCgThreads>(partials, gridDim.x, sm);
+    const double sigma = reduce_partials<false, kCgThreads>(partials + kMaxBlocks, gridDim.x, sm);
     if (threadIdx.x == 0) {
         st->counter[0] = 0;
         // The stop test compares in T, as pcg.rs:35 / :60 do.
@@ -82,7 +81,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
         st->threshold = t;
         st->bmax = bmax;
         st->rmax = bmax;
-        st->sigma = sigma;
+        st->sigma = sigma;  // PM_ZBUF: set later by the preconditioner
         st->beta = 0.0;
         st->iter = 0;
         st->max_iter = max_iter;
@@ -92,7 +91,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
         if (st->nan_seen || !isfinite(sigma)) {
             st->status = PG_NAN_DETECTED;
             st->done = 1;
-        } else if ((T)bmax < (T)t) {  // early out, pcg.rs:35-38
+        } else if ((T)bmax < (T)t || bmax == 0.0) {  // early out, pcg.rs:35-38 (b = 0: x = 0 is exact)
             st->status = PG_OK;
             st->done = 1;
         } else if (max_iter <= 0) {
@@ -102,24 +101,25 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
 }
 
 // Fused search-direction update and operator application.
-template <class T, int ND, int PRE>
+template <class T, int ND, int PM>
 __global__ void __launch_bounds__(kCgThreads)
-    k_cg_spmv(const T* __restrict__ r, const T* __restrict__ p_old, T* __restrict__ p_new, T* __restrict__ ap,
-              const uint8_t* __restrict__ flags, Dims D, T dt, CgState* st, double* partials) {
+    k_cg_spmv(const T* __restrict__ r, const T* __restrict__ zb, const T* __restrict__ p_old, T* __restrict__ p_new,
+              T* __restrict__ ap, const uint8_t* __restrict__ flags, Dims D, T dt, CgState* st, double* partials) {
     if (st->done) return;
     __shared__ double sm[32];
     const int first = st->first;
-    const T beta = (T)st->beta;
+    const T beta = first ? T(0) : (T)st->beta;
     const i64 n = D.nc(), w = D.w, hw = D.h * D.w;
     auto pn = [&](i64 k) -> T {
-        const T z = precond_apply<T, PRE>(r[k], PRE ? flags[k] : 0, dt);
+        const T z = zval<T, PM>(r, flags, zb, k, dt);
         return first ? z : z + beta * p_old[k];
     };
-    double acc = 0.0;
+    Acc<T> acc;
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
         const uint8_t f = flags[c];
         const T pc = pn(c);
         p_new[c] = pc;
+        // Reference operator order (grid.rs:295-335 after *1^-1).
         const T gy_lo = (f & YLO) ? -sub_rn(pc, pn(c - w)) : T(0);
         const T gy_hi = (f & YHI) ? -sub_rn(pn(c + w), pc) : T(0);
         const T gx_lo = (f & XLO) ? sub_rn(pn(c - 1), pc) : T(0);
@@ -132,12 +132,12 @@ __global__ void __launch_bounds__(kCgThreads)
         }
         const T a = mul_rn(v, dt);
         ap[c] = a;
-        acc += (double)pc * (double)a;
+        acc.add(pc * a);
     }
-    const double s = block_sum<kCgThreads>(acc, sm);
+    const double s = block_sum<kCgThreads>(acc.value(), sm);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
     if (!last_block(&st->counter[1])) return;
-    const double pap = reduce_partials<false>(partials, gridDim.x, sm);
+    const double pap = reduce_partials<false, kCgThreads>(partials, gridDim.x, sm);
     if (threadIdx.x == 0) {
         st->counter[1] = 0;
         st->pap = pap;
@@ -153,83 +153,88 @@ __global__ void __launch_bounds__(kCgThreads)
     }
 }
 
-template <class T, int PRE>
+template <class T, int PM>
 __global__ void __launch_bounds__(kCgThreads)
     k_cg_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ ap,
                 const uint8_t* __restrict__ flags, i64 n, T dt, CgState* st, double* partials) {
     if (st->done) return;
     __shared__ double sm[32];
     const T alpha = (T)st->alpha, nalpha = -alpha;
-    double rm = 0.0, rz = 0.0;
+    T rm = T(0);
+    Acc<T> rz;
     int bad = 0;
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
         x[c] = x[c] + alpha * p[c];          // pcg.rs:55
         const T rv = r[c] + nalpha * ap[c];  // pcg.rs:56
         r[c] = rv;
-        const T z = precond_apply<T, PRE>(rv, PRE ? flags[c] : 0, dt);
-        rm = fmax(rm, fabs((double)rv));
-        rz += (double)z * (double)rv;
+        rm = fmax(rm, fabs(rv));
         bad |= !isfinite(rv);
+        if (PM != PM_ZBUF) rz.add(zof<T, PM>(rv, flags, c, dt) * rv);
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
-    const double m = block_max<kCgThreads>(rm, sm);
-    const double s = block_sum<kCgThreads>(rz, sm);
+    const double m = block_max<kCgThreads>((double)rm, sm);
+    const double s = block_sum<kCgThreads>(rz.value(), sm);
     if (threadIdx.x == 0) {
         partials[2 * kMaxBlocks + blockIdx.x] = m;
         partials[3 * kMaxBlocks + blockIdx.x] = s;
     }
     if (!last_block(&st->counter[2])) return;
-    const double rmax = reduce_partials<true>(partials + 2 * kMaxBlocks, gridDim.x, sm);
-    const double sigma_new = reduce_partials<false>(partials + 3 * kMaxBlocks, gridDim.x, sm);
+    const double rmax = reduce_partials<true, kCgThreads>(partials + 2 * kMaxBlocks, gridDim.x, sm);
+    const double sigma_new = reduce_partials<false, kCgThreads>(partials + 3 * kMaxBlocks, gridDim.x, sm);
     if (threadIdx.x == 0) {
         st->counter[2] = 0;
         const i64 it = st->iter + 1;
         st->iter = it;
         st->rmax = rmax;
-        if (st->nan_seen || !isfinite(sigma_new)) {
+        if (st->nan_seen || !isfinite(rmax)) {
             st->status = PG_NAN_DETECTED;
             st->done = 1;
         } else if ((T)rmax < (T)st->threshold) {  // pcg.rs:58-63
             st->status = PG_OK;
             st->done = 1;
         } else {
-            st->beta = sigma_new / st->sigma;  // pcg.rs:67-68
-            st->sigma = sigma_new;
-            st->first = 0;
-            if (it >= st->max_iter) st->done = 1;  // loop bound, pcg.rs:48
+            if (PM != PM_ZBUF) cg_finish_rz(st, sigma_new);  // pcg.rs:65-68
+            if (it >= st->max_iter) st->done = 1;          // loop bound, pcg.rs:48
         }
     }
 }
 
 // After max_iterations the reference has already run aux = M r and
 // search = aux + beta*search (pcg.rs:65-77); reproduce that tail.
-template <class T, int PRE>
+template <class T, int PM>
 __global__ void k_cg_tail(const T* __restrict__ r, const T* __restrict__ p, T* __restrict__ aux, T* __restrict__ search,
                           const uint8_t* __restrict__ flags, i64 n, T dt, const CgState* st) {
     const T beta = (T)st->beta;
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
-        const T z = precond_apply<T, PRE>(r[c], PRE ? flags[c] : 0, dt);
+        const T z = zof<T, PM>(r[c], flags, c, dt);
         const T pv = p[c];
         aux[c] = z;
         search[c] = z + beta * pv;
     }
 }
 
-template <class T, int PRE> static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, i64 k, T dt, int nb) {
+template <class T, int PM>
+static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, i64 k, T dt, int nb, ZHook* hook) {
     const Dims& D = g->dims;
     T* p_old = buf.p[k & 1];
     T* p_new = buf.p[(k + 1) & 1];
+    cudaStream_t s = g->stream;
     if (D.nd == 2)
-        k_cg_spmv<T, 2, PRE><<<nb, kCgThreads, 0, g->stream>>>(buf.r, p_old, p_new, buf.ap, g->flags, D, dt,
-                                                               g->ws.state, g->ws.partials);
+        PG_LAUNCH(KK_CG_SPMV, s,
+                  k_cg_spmv<T, 2, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, p_old, p_new, buf.ap, g->flags, D, dt,
+                                                                g->ws.state, g->ws.partials));
     else
-        k_cg_spmv<T, 3, PRE><<<nb, kCgThreads, 0, g->stream>>>(buf.r, p_old, p_new, buf.ap, g->flags, D, dt,
-                                                               g->ws.state, g->ws.partials);
-    k_cg_update<T, PRE><<<nb, kCgThreads, 0, g->stream>>>(buf.x, buf.r, p_new, buf.ap, g->flags, D.nc(), dt,
-                                                          g->ws.state, g->ws.partials);
+        PG_LAUNCH(KK_CG_SPMV, s,
+                  k_cg_spmv<T, 3, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, p_old, p_new, buf.ap, g->flags, D, dt,
+                                                                g->ws.state, g->ws.partials));
+    PG_LAUNCH(KK_CG_UPDATE, s,
+              k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, p_new, buf.ap, g->flags, D.nc(), dt,
+                                                           g->ws.state, g->ws.partials));
+    if (PM == PM_ZBUF) hook->apply(g, buf.r, buf.z);
 }
 
-template <class T> int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stats) {
+template <class T, int PM>
+static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stats, ZHook* hook) {
     int rc = ensure_workspace(g);
     if (rc) return rc;
     const Dims& D = g->dims;
@@ -237,36 +242,31 @@ template <class T> int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf,
     const T dt = (T)cfg.dt;
     const int nb = grid_blocks(g, n, kCgThreads, 8);
     Workspace& ws = g->ws;
-    const bool jac = cfg.precond == PG_PRECOND_JACOBI;
-    PG_CUDA(cudaMemsetAsync(ws.state, 0, sizeof(CgState), g->stream));
-    if (jac)
-        k_cg_init<T, PG_PRECOND_JACOBI><<<nb, kCgThreads, 0, g->stream>>>(buf.x, buf.r, buf.b, g->flags, n, dt,
-                                                                           cfg.threshold, cfg.rel_tol, cfg.max_iter,
-                                                                           cfg.zero_x, ws.state, ws.partials);
-    else
-        k_cg_init<T, PG_PRECOND_NONE><<<nb, kCgThreads, 0, g->stream>>>(buf.x, buf.r, buf.b, g->flags, n, dt,
-                                                                         cfg.threshold, cfg.rel_tol, cfg.max_iter,
-                                                                         cfg.zero_x, ws.state, ws.partials);
+    cudaStream_t s = g->stream;
+    PG_CUDA(cudaMemsetAsync(ws.state, 0, sizeof(CgState), s));
+    PG_LAUNCH(KK_CG_INIT, s,
+              k_cg_init<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.b, g->flags, n, dt, cfg.threshold,
+                                                         cfg.rel_tol, cfg.max_iter, cfg.zero_x, ws.state,
+                                                         ws.partials));
     PG_CHECK_LAUNCH();
+    if (PM == PM_ZBUF && (rc = hook->apply(g, buf.r, buf.z))) return rc;
     // Poll interval: about 0.5 ms of device work per chunk.
     int chunk = cfg.check_every;
     if (chunk <= 0) {
-        const double us_per_iter = 3.0 + (double)n * 45.0 / 6.0e6;  // launch floor + HBM time
-        chunk = (int)std::min(64.0, std::max(4.0, 500.0 / us_per_iter));
+        double us_per_iter = 4.0 + (double)n * 41.0 / 5.0e6;  // launch floor + HBM time
+        if (PM == PM_ZBUF) us_per_iter = 3.0 * us_per_iter + 100.0;
+        chunk = (int)std::min(64.0, std::max(2.0, 600.0 / us_per_iter));
     }
     i64 launched = 0;
     int slot = 0, pending = -1;
     bool done = false;
     while (!done && launched < cfg.max_iter) {
         const i64 todo = std::min<i64>(chunk, cfg.max_iter - launched);
-        for (i64 k = 0; k < todo; ++k) {
-            if (jac) launch_iter<T, PG_PRECOND_JACOBI>(g, buf, launched + k, dt, nb);
-            else launch_iter<T, PG_PRECOND_NONE>(g, buf, launched + k, dt, nb);
-        }
+        for (i64 k = 0; k < todo; ++k) launch_iter<T, PM>(g, buf, launched + k, dt, nb, hook);
         PG_CHECK_LAUNCH();
         launched += todo;
-        PG_CUDA(cudaMemcpyAsync(ws.state_host + slot, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost, g->stream));
-        PG_CUDA(cudaEventRecord(ws.ev[slot], g->stream));
+        PG_CUDA(cudaMemcpyAsync(ws.state_host + slot, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+        PG_CUDA(cudaEventRecord(ws.ev[slot], s));
         if (pending >= 0) {
             PG_CUDA(cudaEventSynchronize(ws.ev[pending]));
             done = ws.state_host[pending].done != 0;
@@ -274,23 +274,33 @@ template <class T> int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf,
         pending = slot;
         slot ^= 1;
     }
-    PG_CUDA(cudaStreamSynchronize(g->stream));
-    CgState s;
-    PG_CUDA(cudaMemcpy(&s, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost));
+    PG_CUDA(cudaStreamSynchronize(s));
+    CgState st;
+    PG_CUDA(cudaMemcpy(&st, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost));
     if (stats) {
-        stats->iterations = s.iter;
+        stats->iterations = st.iter;
         stats->refinements = 0;
-        stats->residual_max = s.rmax;
-        stats->b_max = s.bmax;
-        stats->threshold = s.threshold;
+        stats->residual_max = st.rmax;
+        stats->b_max = st.bmax;
+        stats->threshold = st.threshold;
         stats->true_residual_max = -1.0;
-        stats->status = s.status;
+        stats->status = st.status;
     }
     return PG_OK;
 }
 
-template int run_cg<float>(pg_grid*, const CgConfig&, CgBuffers<float>, pg_pcg_stats*);
-template int run_cg<double>(pg_grid*, const CgConfig&, CgBuffers<double>, pg_pcg_stats*);
+template <class T>
+int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stats, ZHook* hook) {
+    if (cfg.precond == PG_PRECOND_MG) {
+        if (!hook || !buf.z) return bad_arg("run_cg: MG preconditioning needs a hook and a z buffer");
+        return run_cg_pm<T, PM_ZBUF>(g, cfg, buf, stats, hook);
+    }
+    if (cfg.precond == PG_PRECOND_JACOBI) return run_cg_pm<T, PM_JACOBI>(g, cfg, buf, stats, nullptr);
+    return run_cg_pm<T, PM_NONE>(g, cfg, buf, stats, nullptr);
+}
+
+template int run_cg<float>(pg_grid*, const CgConfig&, CgBuffers<float>, pg_pcg_stats*, ZHook*);
+template int run_cg<double>(pg_grid*, const CgConfig&, CgBuffers<double>, pg_pcg_stats*, ZHook*);
 
 // pg_pcg_*: the reference signature with caller-owned work vectors.
 template <class T>
@@ -318,18 +328,21 @@ static int pcg_abi(const pg_grid* cg, int precond, T* x, const T* b, int64_t max
     const i64 it = st.iterations;
     T* p_cur = buf.p[it & 1];
     const int nb = grid_blocks(g, n, kCgThreads, 8);
+    cudaStream_t s = g->stream;
     if (it > 0 && st.status == PG_NOT_CONVERGED && it >= max_iter) {
         if (precond == PG_PRECOND_JACOBI)
-            k_cg_tail<T, PG_PRECOND_JACOBI><<<nb, kCgThreads, 0, g->stream>>>(residual, p_cur, auxiliary, search,
-                                                                             g->flags, n, (T)dt, g->ws.state);
+            PG_LAUNCH(KK_CG_TAIL, s,
+                      k_cg_tail<T, PM_JACOBI><<<nb, kCgThreads, 0, s>>>(residual, p_cur, auxiliary, search, g->flags,
+                                                                       n, (T)dt, g->ws.state));
         else
-            k_cg_tail<T, PG_PRECOND_NONE><<<nb, kCgThreads, 0, g->stream>>>(residual, p_cur, auxiliary, search,
-                                                                           g->flags, n, (T)dt, g->ws.state);
+            PG_LAUNCH(KK_CG_TAIL, s,
+                      k_cg_tail<T, PM_NONE><<<nb, kCgThreads, 0, s>>>(residual, p_cur, auxiliary, search, g->flags, n,
+                                                                     (T)dt, g->ws.state));
         PG_CHECK_LAUNCH();
     } else if (it > 0 && p_cur != search) {
-        PG_CUDA(cudaMemcpyAsync(search, p_cur, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, g->stream));
+        PG_CUDA(cudaMemcpyAsync(search, p_cur, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
     }
-    PG_CUDA(cudaStreamSynchronize(g->stream));
+    PG_CUDA(cudaStreamSynchronize(s));
     if (stats) *stats = st;
     return st.status;
 }

@@ -4,6 +4,9 @@
 
 namespace pg {
 
+// How z = M^-1 r is obtained inside the CG kernels.
+enum PrecMode { PM_NONE = 0, PM_JACOBI = 1, PM_ZBUF = 2 /* z stored by an outer preconditioner (MG) */ };
+
 // Buffers of one CG run.  p[0], p[1] ping-pong: the SpMV of iteration k
 // reads p[k & 1] and writes p[(k + 1) & 1], so the search direction of the
 // latest iteration is p[iter & 1].
@@ -13,10 +16,11 @@ template <class T> struct CgBuffers {
     T* r;
     T* ap;
     T* p[2];
+    T* z = nullptr;  // PM_ZBUF only
 };
 
 struct CgConfig {
-    int precond;        // PG_PRECOND_NONE or PG_PRECOND_JACOBI
+    int precond;        // PG_PRECOND_NONE / JACOBI / MG
     i64 max_iter;
     double threshold;   // absolute: stop when ||r||inf < threshold
     double rel_tol;     // > 0: threshold = rel_tol * ||b||inf (set on device)
@@ -25,8 +29,79 @@ struct CgConfig {
     int zero_x;         // 1: x = 0 first (pcg.rs:32)
 };
 
+// Per-thread partial sums: compensated FP32 (float fields) or plain FP64
+// (double fields); the cross-thread/-block tree is FP64 in both cases.
+template <class T> struct Acc;
+template <> struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <> struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+// Hooks for an outer preconditioner that produces z between the update
+// and the next SpMV (multigrid).  The last V-cycle kernel reduces z.r and
+// calls cg_finish_rz on the device state.
+struct ZHook {
+    // Enqueue z = M^-1 r on the grid's stream; must end with a kernel that
+    // publishes z.r through cg_finish_rz.
+    virtual int apply(pg_grid* g, const void* r, void* z) = 0;
+    virtual ~ZHook() {}
+};
+
 // Runs CG on the grid's stream and synchronises at the end.  Returns a
 // pg_status for launch/CUDA failures; the solve outcome is in *stats.
-template <class T> int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stats);
+template <class T>
+int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stats, ZHook* hook = nullptr);
+
+// Device side: fold a freshly reduced z.r into the CG state.  Right after
+// init (iter == 0) it is sigma; afterwards beta = z.r / sigma (pcg.rs:67-68).
+__device__ __forceinline__ void cg_finish_rz(CgState* st, double rz) {
+    if (st->done) return;
+    if (!isfinite(rz)) {
+        st->status = PG_NAN_DETECTED;
+        st->done = 1;
+        return;
+    }
+    if (st->iter == 0) {
+        st->sigma = rz;
+    } else {
+        st->beta = rz / st->sigma;
+        st->sigma = rz;
+        st->first = 0;
+    }
+}
+
+// Last-block ticket: true in every thread of the block that finished last.
+// Per-block partials must be written (by thread 0) before the call.
+__device__ __forceinline__ bool last_block(unsigned int* counter) {
+    __shared__ bool am_last;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        const unsigned int t = atomicAdd(counter, 1u);
+        am_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return am_last;
+}
+
+// Deterministic sum (or max) of n per-block partials, by one block of NT.
+template <bool MAX, int NT> __device__ __forceinline__ double reduce_partials(const double* partials, int n, double* sm) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double pv = __ldcg(partials + i);
+        v = MAX ? fmax(v, pv) : v + pv;
+    }
+    return MAX ? block_max<NT>(v, sm) : block_sum<NT>(v, sm);
+}
 
 }  // namespace pg

@@ -139,13 +139,15 @@ __global__ void k_rhs(T* __restrict__ b, const T* __restrict__ vel, const uint8_
 // Projection of examples/dec_fluid.rs:123-141: interior faces
 // vel = vel + dt * e (scaled_add) with e from grid.rs:318-334, boundary
 // faces zeroed (walls).  zero_solid: solid interior faces zeroed after.
-template <class T>
-__global__ void k_project(T* __restrict__ vel, const T* __restrict__ p, const uint8_t* __restrict__ flags, Dims D, T dt,
+// P is the pressure type: T (the reference's arithmetic), or double for a
+// float field projected with the FP64 pressure of the refined solve.
+template <class T, class P>
+__global__ void k_project(T* __restrict__ vel, const P* __restrict__ p, const uint8_t* __restrict__ flags, Dims D, P dt,
                           int zero_solid) {
     const i64 nz = D.nfz(), ny = D.nfy(), nf = D.nf();
     const i64 h = D.h, w = D.w, hw = h * w;
     GRID_STRIDE(i, nf) {
-        T e;
+        P e;
         bool open;
         if (i < nz) {
             const i64 z = i / hw, r = i - z * hw;
@@ -169,7 +171,7 @@ __global__ void k_project(T* __restrict__ vel, const T* __restrict__ p, const ui
             e = sub_rn(p[c - 1], p[c]);
             open = flags[c] & XLO;
         }
-        vel[i] = (zero_solid && !open) ? T(0) : add_rn(vel[i], mul_rn(dt, e));
+        vel[i] = (zero_solid && !open) ? T(0) : add_rn(vel[i], (T)mul_rn(dt, e));
     }
 }
 
@@ -233,13 +235,13 @@ template <class T> __global__ void k_buoyancy(T* __restrict__ vel, const T* __re
 template <class T> int launch_hodge1(const pg_grid* g, T* out, const T* in, int neg_first) {
     const Dims& D = g->dims;
     const i64 n0 = D.nfy(), n = D.nf();
-    k_hodge1<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(out, in, n0, n, neg_first);
+    PG_LAUNCH(KK_DEC_OP, g->stream, k_hodge1<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(out, in, n0, n, neg_first));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_copy(const pg_grid* g, T* out, const T* in, i64 n) {
-    k_copy<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(out, in, n);
+    PG_LAUNCH(KK_DEC_OP, g->stream, k_copy<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(out, in, n));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -247,9 +249,9 @@ template <class T> int launch_copy(const pg_grid* g, T* out, const T* in, i64 n)
 template <class T> int launch_laplacian(const pg_grid* g, T* out, const T* p, double dt) {
     const Dims& D = g->dims;
     if (D.nd == 2)
-        k_laplacian<T, 2><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(out, p, g->flags, D, (T)dt);
+        PG_LAUNCH(KK_DEC_OP, g->stream, k_laplacian<T, 2><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(out, p, g->flags, D, (T)dt));
     else
-        k_laplacian<T, 3><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(out, p, g->flags, D, (T)dt);
+        PG_LAUNCH(KK_DEC_OP, g->stream, k_laplacian<T, 3><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(out, p, g->flags, D, (T)dt));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -257,23 +259,32 @@ template <class T> int launch_laplacian(const pg_grid* g, T* out, const T* p, do
 template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel) {
     const Dims& D = g->dims;
     if (D.nd == 2)
-        k_rhs<T, 2><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D);
+        PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 2><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D));
     else
-        k_rhs<T, 3><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D);
+        PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 3><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid) {
     const Dims& D = g->dims;
-    k_project<T><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, p, g->flags, D, (T)dt, zero_solid);
+    PG_LAUNCH(KK_PROJECT, g->stream, k_project<T, T><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, p, g->flags, D, (T)dt, zero_solid));
+    PG_CHECK_LAUNCH();
+    return PG_OK;
+}
+
+int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid) {
+    const Dims& D = g->dims;
+    PG_LAUNCH(KK_PROJECT, g->stream,
+              k_project<float, double><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
+                  vel, p, g->flags, D, dt, zero_solid));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_walls(const pg_grid* g, T* vel) {
     const Dims& D = g->dims;
-    k_walls<T><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, D);
+    PG_LAUNCH(KK_DEC_OP, g->stream, k_walls<T><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, D));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -290,23 +301,23 @@ template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const
     }
     const i64 n = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
     if (n == 0) return PG_OK;
-    k_source_box<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(
+    PG_LAUNCH(KK_STEP_MISC, g->stream, k_source_box<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(
         rho, vel, D, lo[0], lo[1], lo[2], hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], (T)prm->source_density,
-        (T)prm->source_vy);
+        (T)prm->source_vy));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* src) {
     const i64 n = g->dims.nc();
-    k_source_field<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(rho, src, n);
+    PG_LAUNCH(KK_STEP_MISC, g->stream, k_source_field<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(rho, src, n));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_buoyancy(const pg_grid* g, T* vel, const T* rho, double dt, double beta) {
     const Dims& D = g->dims;
-    k_buoyancy<T><<<grid_blocks(g, D.nfy(), kThreads), kThreads, 0, g->stream>>>(vel, rho, D, (T)(dt * beta));
+    PG_LAUNCH(KK_STEP_MISC, g->stream, k_buoyancy<T><<<grid_blocks(g, D.nfy(), kThreads), kThreads, 0, g->stream>>>(vel, rho, D, (T)(dt * beta)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -350,15 +361,15 @@ using namespace pg;
         NEED(g && faces && edges, "pg_derivative_1_primal: NULL argument");                                 \
         NEED(g->dims.nd == 2, "pg_derivative_1_primal: 2D grids only");                                     \
         const i64 n = g->dims.nc();                                                                         \
-        k_d1primal_2d<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(faces, edges, g->dims.h,  \
-                                                                                  g->dims.w);               \
+        PG_LAUNCH(KK_DEC_OP, g->stream, k_d1primal_2d<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(faces, edges, g->dims.h,  \
+                                                                                  g->dims.w));               \
         PG_CHECK_LAUNCH();                                                                                  \
         return PG_OK;                                                                                       \
     }                                                                                                       \
     extern "C" int pg_derivative_0_dual_##SFX(const pg_grid* g, T* edges, const T* faces) {                \
         NEED(g && faces && edges, "pg_derivative_0_dual: NULL argument");                                   \
         const i64 n = g->dims.nf();                                                                         \
-        k_d0dual<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(edges, faces, g->dims);        \
+        PG_LAUNCH(KK_DEC_OP, g->stream, k_d0dual<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(edges, faces, g->dims));        \
         PG_CHECK_LAUNCH();                                                                                  \
         return PG_OK;                                                                                       \
     }                                                                                                       \
@@ -366,7 +377,7 @@ using namespace pg;
         NEED(g && edges, "pg_mask_solid_faces: NULL argument");                                             \
         if (!g->face_solid) return PG_OK;                                                                   \
         const i64 n = g->dims.nf();                                                                         \
-        k_mask<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(edges, g->face_solid, n);        \
+        PG_LAUNCH(KK_DEC_OP, g->stream, k_mask<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(edges, g->face_solid, n));        \
         PG_CHECK_LAUNCH();                                                                                  \
         return PG_OK;                                                                                       \
     }                                                                                                       \

@@ -70,6 +70,7 @@ static int upload_mask(pg_grid* g, const uint8_t* host_face_solid) {
     const Dims& D = g->dims;
     std::vector<uint8_t> flags;
     build_flags(D, host_face_solid, flags);
+    ++g->mask_version;
     PG_CUDA(cudaMemcpy(g->flags, flags.data(), flags.size(), cudaMemcpyHostToDevice));
     if (host_face_solid) {
         if (!g->face_solid) PG_CUDA(cudaMalloc(&g->face_solid, (size_t)D.nf()));

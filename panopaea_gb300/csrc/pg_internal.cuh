@@ -119,6 +119,7 @@ struct pg_grid {
     int num_sms = 0;
     uint8_t* flags = nullptr;       // device, per cell: Laplacian face-open bits
     uint8_t* face_solid = nullptr;  // device, per face (1 = solid) or null
+    unsigned long long mask_version = 0;  // bumped on every mask upload
     pg::Workspace ws;
     void* extras = nullptr;         // solver state owned by pg_solve.cu (MG levels, graphs)
 };
@@ -151,6 +152,23 @@ inline int grid_blocks(const pg_grid* g, i64 n, int threads, int per_sm = 8) {
     if (b < 1) b = 1;
     return (int)b;
 }
+
+// Kernel kinds for launch counting and event timing (pg_prof.cu).
+enum KernelKind {
+    KK_CG_INIT, KK_CG_SPMV, KK_CG_UPDATE, KK_CG_TAIL, KK_ADVECT, KK_ADVECT_MAC, KK_RHS, KK_PROJECT, KK_DEC_OP,
+    KK_RESIDUAL64, KK_REFINE_UPDATE, KK_MG_SMOOTH, KK_MG_RESTRICT, KK_MG_SMOOTH_C, KK_MG_RESTRICT_C, KK_MG_COARSE,
+    KK_MG_SETUP, KK_STEP_MISC, KK_COUNT
+};
+void prof_begin(cudaStream_t s, int kind);
+void prof_end(cudaStream_t s, int kind);
+
+// Every kernel launch of the library goes through this macro.
+#define PG_LAUNCH(kind, stream, ...)        \
+    do {                                    \
+        ::pg::prof_begin((stream), (kind)); \
+        __VA_ARGS__;                        \
+        ::pg::prof_end((stream), (kind));   \
+    } while (0)
 
 int ensure_workspace(pg_grid* g);
 void release_extras(pg_grid* g);

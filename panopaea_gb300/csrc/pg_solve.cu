@@ -12,6 +12,7 @@ namespace pg {
 template <class T> int launch_copy(const pg_grid* g, T* out, const T* in, i64 n);
 template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel);
 template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid);
+int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid);
 template <class T> int launch_walls(const pg_grid* g, T* vel);
 template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const pg_step_params* prm);
 template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* src);
@@ -113,9 +114,9 @@ static int residual64(pg_grid* g, const float* b, const double* x, double dt, fl
     double* dev_out = (double*)ex->small;
     unsigned int* counter = (unsigned int*)(dev_out + 1);
     if (D.nd == 2)
-        k_residual64<2><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out);
+        PG_LAUNCH(KK_RESIDUAL64, g->stream, k_residual64<2><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
     else
-        k_residual64<3><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out);
+        PG_LAUNCH(KK_RESIDUAL64, g->stream, k_residual64<3><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaMemcpyAsync(rmax_host, dev_out, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
     PG_CUDA(cudaStreamSynchronize(g->stream));
@@ -193,7 +194,7 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
                 out.status = s.status;
                 break;
             }
-            k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n);
+            PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
             PG_CHECK_LAUNCH();
             if ((rc = residual64(g, b, (const double*)x64, dt, (float*)rin, &rmax))) return rc;
             if (!std::isfinite(rmax)) {
@@ -210,7 +211,7 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     } else {
         out.status = PG_OK;
     }
-    k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n);
+    PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n));
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(g->stream));
     out.iterations = iters;
@@ -260,8 +261,16 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure, pg_
     // pressure solve (dec_fluid.rs:87-121)
     pg_pcg_stats s{};
     if ((rc = solve_pressure<T>(g, &prm->solver, pressure, (const T*)b, dt, &s))) return rc;
-    // projection + walls (dec_fluid.rs:123-141)
-    if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project))) return rc;
+    // projection + walls (dec_fluid.rs:123-141); after a refined solve the
+    // gradient is taken from the FP64 pressure it accumulated.
+    if (sizeof(T) == 4 && prm->solver.refine > 0) {
+        void* x64;
+        if ((rc = ex->buffer(Extras::kX64, sizeof(double) * nc, &x64))) return rc;
+        if ((rc = launch_project_p64(g, (float*)vel, (const double*)x64, dt, prm->zero_solid_after_project)))
+            return rc;
+    } else if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project))) {
+        return rc;
+    }
     PG_CUDA(cudaStreamSynchronize(g->stream));
     if (st) *st = s;
     return s.status;

@@ -1,0 +1,98 @@
+"""Seeded synthetic inputs for the benchmark configurations (numpy only, so
+every process that builds them gets identical arrays).
+
+* :func:`filtered_noise_velocity` -- faces i.i.d. N(0, 1) (seeded), low-pass
+  filtered by 3 passes of a 3x3x3 box filter per face array, scaled to
+  max|u| = umax, boundary faces zeroed (solid walls);
+* :func:`filtered_noise_density` -- a cell field built the same way, mapped
+  affinely onto [0, 1];
+* :func:`gaussian_blob_2d` -- exp(-|x - c|^2 / (2 sigma^2)), c and sigma as
+  fractions of the domain, peak 1.
+"""
+
+import numpy as np
+
+
+def _box3(a, passes=3):
+    """`passes` passes of a 3-wide box filter along every axis (edge values
+    repeated at the borders)."""
+    a = np.asarray(a, np.float32)
+    for _ in range(passes):
+        for ax in range(a.ndim):
+            pad = [(0, 0)] * a.ndim
+            pad[ax] = (1, 1)
+            p = np.pad(a, pad, mode="edge")
+            n = a.shape[ax]
+            sl = lambda s, e: tuple(slice(s, e) if i == ax else slice(None) for i in range(a.ndim))  # noqa: E731
+            a = (p[sl(0, n)] + p[sl(1, n + 1)] + p[sl(2, n + 2)]) * np.float32(1.0 / 3.0)
+    return a
+
+
+def face_shapes(dims):
+    if len(dims) == 2:
+        h, w = dims
+        return [(h + 1, w), (h, w + 1)]
+    d, h, w = dims
+    return [(d + 1, h, w), (d, h + 1, w), (d, h, w + 1)]
+
+
+def num_faces(dims):
+    return sum(int(np.prod(s)) for s in face_shapes(dims))
+
+
+def zero_walls(parts):
+    """Zero the domain-boundary faces of each face part (normal axis ends)."""
+    nd = parts[0].ndim
+    for ax, part in enumerate(parts):  # part k is normal to axis k ((z,) y, x order)
+        idx0 = tuple(0 if i == ax else slice(None) for i in range(nd))
+        idx1 = tuple(-1 if i == ax else slice(None) for i in range(nd))
+        part[idx0] = 0.0
+        part[idx1] = 0.0
+    return parts
+
+
+def filtered_noise_velocity(dims, seed=2, umax=2.0, passes=3, dtype=np.float32):
+    rng = np.random.default_rng(seed)
+    parts = [_box3(rng.standard_normal(s, dtype=np.float32), passes) for s in face_shapes(dims)]
+    zero_walls(parts)
+    m = max(np.abs(p).max() for p in parts)
+    parts = [p * (umax / m) for p in parts]
+    return np.concatenate([p.ravel() for p in parts]).astype(dtype)
+
+
+def filtered_noise_density(dims, seed=3, passes=3, dtype=np.float32):
+    rng = np.random.default_rng(seed)
+    a = _box3(rng.standard_normal(dims, dtype=np.float32), passes)
+    a = (a - a.min()) / (a.max() - a.min())
+    return a.astype(dtype)
+
+
+def gaussian_blob_2d(dims, center=(0.5, 0.15), sigma=0.04, dtype=np.float32):
+    """center = (x, y) fractions (y up), sigma a fraction of the larger side."""
+    h, w = dims
+    s = sigma * max(h, w)
+    y, x = np.mgrid[0:h, 0:w]
+    cx, cy = center[0] * w, center[1] * h
+    return np.exp(-(((x + 0.5 - cx) ** 2 + (y + 0.5 - cy) ** 2) / (2 * s * s))).astype(dtype)
+
+
+# Named workloads: dims, dt and the fields they start from.
+WORKLOADS = {
+    # 3D MAC grid 256^3, filtered-noise velocity (max |u| = 2 cells/step, so
+    # dt = 1), walls, one step of trilinear advection + 7-point projection
+    # to relative residual 1e-6.
+    "precision_3d_256": dict(dims=(256, 256, 256), dt=1.0, rel_tol=1e-6, buoyancy=0.0),
+    # 2D plume 256^2: blob at (0.5, 0.15), sigma 0.04, buoyancy 1, dt 0.5, 1e-5.
+    "plume_2d_256": dict(dims=(256, 256), dt=0.5, rel_tol=1e-5, buoyancy=1.0),
+}
+
+
+def initial_state(name, dims=None):
+    """(vel, density) host arrays for a named workload (dims overridable)."""
+    spec = WORKLOADS[name]
+    dims = tuple(dims or spec["dims"])
+    if name.startswith("plume_2d"):
+        vel = np.zeros(num_faces(dims), np.float32)
+        rho = gaussian_blob_2d(dims)
+        return vel, rho
+    return filtered_noise_velocity(dims), filtered_noise_density(dims)

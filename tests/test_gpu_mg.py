@@ -1,0 +1,105 @@
+"""Multigrid-preconditioned CG (an extension behind pcg.rs:4-6
+`Preconditioner`): converges in a grid-size-independent handful of
+iterations, to the same solution as the oracle's CG, with obstacles, odd and
+anisotropic shapes, in 2D and 3D."""
+
+import numpy as np
+import pytest
+
+from conftest import rng, seed_of
+from test_gpu_ops import cells, faces, host, make_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def solve_case(pg, oracle, dims, obstacle, precond, tol, refine=0):
+    r = rng(seed_of(dims, obstacle))
+    nf = oracle.num_faces(dims)
+    cs = None
+    g = make_grid(pg, dims)
+    if obstacle:
+        idx = np.indices(dims).astype(np.float64)
+        ctr = np.array([(n - 1) / 2 for n in dims]).reshape((-1,) + (1,) * len(dims))
+        cs = (((idx - ctr) ** 2).sum(0) < (min(dims) / 5.0) ** 2).astype(np.uint8)
+        g.set_solid_cells(cs)
+    fs = oracle.cell_mask_to_faces(cs) if obstacle else None
+    vel = oracle.walls(r.standard_normal(nf).astype(np.float32), dims)
+    b = g.new_simplex_2()
+    g.divergence_rhs(b, faces(pg, g, vel))
+    x = g.new_simplex_2()
+    st = pg.solve_pressure(g, x, b, 0.5, pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=tol,
+                                                         max_iter=20000, refine=refine))
+    bh = host(b).astype(np.float64)
+    xh = host(x).astype(np.float64)
+    true_r = np.abs(bh - oracle.laplacian(xh, 0.5, dims, fs)).max() / np.abs(bh).max()
+    return st, xh, bh, true_r, fs
+
+
+@pytest.mark.parametrize("dims", [(64, 64), (256, 256), (200, 131), (33, 47, 29), (64, 64, 64), (128, 128, 128),
+                                  (16, 64, 40), (256, 16)])
+@pytest.mark.parametrize("obstacle", [False, True])
+def test_mgpcg_converges_fast(pg, oracle, dims, obstacle):
+    st, x, b, true_r, fs = solve_case(pg, oracle, dims, obstacle, 2, 1e-5)
+    assert st["status"] == 0, st
+    assert st["iterations"] <= 30, st
+    # FP32 storage: the true residual is within the FP32 floor of x
+    floor = 16 * 2.0 ** -24 * 0.5 * np.abs(x).max() / np.abs(b).max()
+    assert true_r <= 20e-5 + floor
+
+
+@pytest.mark.parametrize("dims", [(128, 128), (48, 40, 36)])
+def test_mgpcg_matches_plain_cg_solution(pg, oracle, dims):
+    """Same projected velocity as plain CG run to the same tolerance (the
+    pressure is unique up to a constant; its gradient is unique)."""
+    st_mg, x_mg, b, _, fs = solve_case(pg, oracle, dims, True, 2, 1e-7, refine=4)
+    st_cg, x_cg, _, _, _ = solve_case(pg, oracle, dims, True, 0, 1e-7, refine=4)
+    assert st_mg["status"] == 0 and st_cg["status"] == 0
+    assert st_mg["iterations"] * 5 < st_cg["iterations"]
+    g_mg = oracle.derivative_0_dual(x_mg, dims)
+    g_cg = oracle.derivative_0_dual(x_cg, dims)
+    assert np.abs(g_mg - g_cg).max() <= 1e-4 * np.abs(g_cg).max()
+
+
+@pytest.mark.parametrize("dims", [(256, 256), (96, 96, 96)])
+def test_refined_mgpcg_reaches_1e6(pg, oracle, dims):
+    st, x, b, true_r, _ = solve_case(pg, oracle, dims, True, 2, 1e-6, refine=5)
+    assert st["status"] == 0 and st["true_residual_max"] <= 1e-6 * st["b_max"], st
+    assert st["iterations"] <= 60
+
+
+def test_mg_rejected_for_f64(pg):
+    """MG is an FP32 preconditioner: an f64 step asking for it is refused."""
+    import torch
+
+    from panopaea_gb300 import _native as N
+
+    g = pg.Grid2d((16, 16))
+    vel, rho, p = g.new_simplex_1(torch.float64), g.new_simplex_2(torch.float64), g.new_simplex_2(torch.float64)
+    rho.data[4, 4] = 1.0
+    vel.data[40] = 1.0
+    cfg = pg.StepConfig(dt=0.5, source_enabled=False, solver=pg.SolverConfig(precond=2, rel_stop=True))
+    with pytest.raises(N.PgError) as ei:
+        pg.step(g, cfg, vel, rho, p)
+    assert ei.value.status == N.PG_BAD_ARG
+    # b = 0 takes the early out before any preconditioner runs
+    st = pg.solve_pressure(g, g.new_simplex_2(), g.new_simplex_2(), 1.0, pg.SolverConfig(precond=2, rel_stop=True))
+    assert st["status"] == 0 and st["iterations"] == 0
+
+
+def test_profile_counters(pg):
+    lib = pg.load()
+    import ctypes as C
+
+    n0 = lib.pg_kernel_launches()
+    g = pg.Grid3d((8, 8, 8))
+    lib.pg_profile_reset()
+    lib.pg_profile_enable(1)
+    out = g.new_simplex_2()
+    g.laplacian(out, g.new_simplex_2(), 1.0)
+    lib.pg_profile_enable(0)
+    assert lib.pg_kernel_launches() > n0
+    names = [lib.pg_profile_kind_name(k).decode() for k in range(lib.pg_profile_num_kinds())]
+    t = C.c_double()
+    n = C.c_int64()
+    lib.pg_profile_read(names.index("dec_op"), C.byref(t), C.byref(n))
+    assert n.value >= 1 and t.value > 0

