@@ -355,7 +355,7 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
     }
     // one allocation for levels >= 1: wx, wy, wz, invd, e, f
     size_t total = 0;
-    for (int l = 1; l < nl; ++l) total += 6 * (size_t)H->lv[l].D.nc() + 64;
+    for (int l = 1; l < nl; ++l) total += 6 * (((size_t)H->lv[l].D.nc() + 63) & ~(size_t)63);
     cudaError_t err = cudaMalloc(&H->mem, std::max<size_t>(total, 1) * sizeof(float));
     if (err != cudaSuccess) {
         delete H;
