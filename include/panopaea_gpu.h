@@ -90,6 +90,11 @@ typedef struct pg_solver_params {
     double inner_rel_tol;  /* per-round relative tolerance with refine > 0 (0 = auto) */
     int32_t mg_levels;     /* MG: number of levels (0 = auto) */
     int32_t mg_smooth;     /* MG: red-black Gauss-Seidel sweeps pre and post (0 = 2) */
+    int32_t fp64_native;   /* refine > 0: 0 = the FP64-class residual, pressure
+                              accumulation and projection run in double-float
+                              (FP32 pairs, ~48-bit significand; GB300 runs
+                              FP64 at 1/64 of the FP32 rate); 1 = native FP64 */
+    int32_t reserved;
 } pg_solver_params;
 
 /* One fluid step, examples/dec_fluid.rs:46-141 (the PNG dump at :143-164

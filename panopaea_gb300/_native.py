@@ -65,6 +65,8 @@ class SolverParams(C.Structure):
         ("inner_rel_tol", C.c_double),
         ("mg_levels", C.c_int32),
         ("mg_smooth", C.c_int32),
+        ("fp64_native", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

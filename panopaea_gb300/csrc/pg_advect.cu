@@ -12,7 +12,7 @@ namespace pg {
 
 constexpr int kThreads = 256;
 
-#define GRID_STRIDE(i, n) for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (i64)gridDim.x * blockDim.x)
+#define GRID_STRIDE(i, n) for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (I)gridDim.x * blockDim.x)
 
 template <class T> __device__ __forceinline__ T bilerp(T a00, T a01, T a10, T a11, T s, T t) {
     return lerp_ref(lerp_ref(a00, a01, s), lerp_ref(a10, a11, s), t);
@@ -21,21 +21,21 @@ template <class T> __device__ __forceinline__ T bilerp(T a00, T a01, T a10, T a1
 // dec_fluid.rs:194-201 for one axis: p = clamp(pos - 0.5, 0, n - 1.00001);
 // i = floor(p); frac = p - i.  `hi` is n - 1.00001 rounded to T; when it
 // rounds to n-1 (float, n >= 257) the index is kept at n-2.
-template <class T> __device__ __forceinline__ void cell_coord(T pos, i64 n, T hi, i64& i0, T& frac) {
+template <class T, class I> __device__ __forceinline__ void cell_coord(T pos, I n, T hi, I& i0, T& frac) {
     const T p = fmin(fmax(sub_rn(pos, T(0.5)), T(0)), hi);
-    i64 i = (i64)floor(p);
+    I i = (I)floor(p);
     if (i > n - 2) i = n - 2;
     i0 = i;
     frac = sub_rn(p, (T)i);
 }
 
 // dec_fluid.rs:236-244 / :274-281 for one axis of a face sample.
-template <class T> __device__ __forceinline__ void face_coord(T pos, T off, i64 n, i64& i0, i64& i1, T& frac) {
+template <class T, class I> __device__ __forceinline__ void face_coord(T pos, T off, I n, I& i0, I& i1, T& frac) {
     const T q = sub_rn(pos, off);
     const T p = fmax(floor(q), T(0));
     const T last = (T)(n - 1);
-    i0 = (i64)fmin(p, last);
-    i1 = (i64)fmin(add_rn(p, T(1)), last);
+    i0 = (I)fmin(p, last);
+    i1 = (I)fmin(add_rn(p, T(1)), last);
     // .min(1.0).max(0.0) with Rust's NaN rule: NaN.min(1) = 1.  Written out
     // because the compiler turns fmax(fmin(v, 1), 0) into a saturate, which
     // maps NaN to 0.
@@ -48,18 +48,18 @@ template <class T> __device__ __forceinline__ T back(T pos, T ndt, T v) { return
 
 // ---------------------------------------------------------------------------
 // advect, 2D (dec_fluid.rs:173-211)
-template <class T>
-__global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, i64 h, i64 w,
+template <class T, class I>
+__global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, I h, I w,
                             T ndt, T hix, T hiy) {
     const T* vy = vel;
     const T* vx = vel + (h + 1) * w;
     GRID_STRIDE(i, h * w) {
-        const i64 y = i / w, x = i - y * w;
+        const I y = i / w, x = i - y * w;
         const T vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), T(2));
         const T vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), T(2));
         const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
         const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
-        i64 ix, iy;
+        I ix, iy;
         T u, v;
         cell_coord(ppx, w, hix, ix, u);
         cell_coord(ppy, h, hiy, iy, v);
@@ -69,24 +69,28 @@ __global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const 
 }
 
 // advect, 3D extension
-template <class T>
+template <class T, class I>
 __global__ void k_advect_3d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, Dims D, T ndt,
                             T hix, T hiy, T hiz) {
-    const i64 h = D.h, w = D.w, hw = h * w;
-    GRID_STRIDE(i, D.nc()) {
-        const i64 zy = i / w, x = i - zy * w;
-        const i64 z = zy / h, y = zy - z * h;
-        const T vcx = div_rn(add_rn(vel[D.fx(z, y, x)], vel[D.fx(z, y, x + 1)]), T(2));
-        const T vcy = div_rn(add_rn(vel[D.fy(z, y, x)], vel[D.fy(z, y + 1, x)]), T(2));
-        const T vcz = div_rn(add_rn(vel[D.fz(z, y, x)], vel[D.fz(z + 1, y, x)]), T(2));
+    const I d = (I)D.d, h = (I)D.h, w = (I)D.w, hw = h * w;
+    const I offy = (I)D.offy(), offx = (I)D.offx();
+    auto FX = [&](I z, I y, I x) { return offx + (z * h + y) * (w + 1) + x; };
+    auto FY = [&](I z, I y, I x) { return offy + (z * (h + 1) + y) * w + x; };
+    auto FZ = [&](I z, I y, I x) { return (z * h + y) * w + x; };
+    GRID_STRIDE(i, d * hw) {
+        const I zy = i / w, x = i - zy * w;
+        const I z = zy / h, y = zy - z * h;
+        const T vcx = div_rn(add_rn(vel[FX(z, y, x)], vel[FX(z, y, x + 1)]), T(2));
+        const T vcy = div_rn(add_rn(vel[FY(z, y, x)], vel[FY(z, y + 1, x)]), T(2));
+        const T vcz = div_rn(add_rn(vel[FZ(z, y, x)], vel[FZ(z + 1, y, x)]), T(2));
         const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
         const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
         const T ppz = back(add_rn((T)z, T(0.5)), ndt, vcz);
-        i64 ix, iy, iz;
+        I ix, iy, iz;
         T s, t, u;
         cell_coord(ppx, w, hix, ix, s);
         cell_coord(ppy, h, hiy, iy, t);
-        cell_coord(ppz, D.d, hiz, iz, u);
+        cell_coord(ppz, d, hiz, iz, u);
         const T* q0 = q + iz * hw + iy * w + ix;
         const T* q1 = q0 + hw;
         dst[i] = lerp_ref(bilerp(q0[0], q0[1], q0[w], q0[w + 1], s, t), bilerp(q1[0], q1[1], q1[w], q1[w + 1], s, t), u);
@@ -95,39 +99,39 @@ __global__ void k_advect_3d(T* __restrict__ dst, const T* __restrict__ q, const 
 
 // ---------------------------------------------------------------------------
 // advect_mac, 2D (dec_fluid.rs:213-291); src/dst/vel share the face layout.
-template <class T>
-__global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, i64 h, i64 w,
+template <class T, class I>
+__global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, I h, I w,
                                 T ndt) {
-    const i64 n0 = (h + 1) * w, nf = n0 + h * (w + 1), wx = w + 1;
+    const I n0 = (h + 1) * w, nf = n0 + h * (w + 1), wx = w + 1;
     const T* vy = vel;
     const T* vx = vel + n0;
     GRID_STRIDE(i, nf) {
         if (i >= n0) {  // x faces, qx dims (h, w+1): dec_fluid.rs:218-253
-            const i64 j = i - n0;
-            const i64 y = j / wx, x = j - y * wx;
-            const i64 xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
+            const I j = i - n0;
+            const I y = j / wx, x = j - y * wx;
+            const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
             const T velx = vx[y * wx + x];
             const T vely = div_rn(add_rn(add_rn(add_rn(vy[y * w + xc], vy[(y + 1) * w + xc]), vy[y * w + xm]),
                                          vy[(y + 1) * w + xm]),
                                   T(4));
             const T ppx = back(add_rn((T)x, T(0)), ndt, velx);
             const T ppy = back(add_rn((T)y, T(0.5)), ndt, vely);
-            i64 x0, x1, y0, y1;
+            I x0, x1, y0, y1;
             T s, t;
             face_coord(ppx, T(0), w + 1, x0, x1, s);
             face_coord(ppy, T(0.5), h, y0, y1, t);
             const T* qx = src + n0;
             dst[i] = bilerp(qx[y0 * wx + x0], qx[y0 * wx + x1], qx[y1 * wx + x0], qx[y1 * wx + x1], s, t);
         } else {  // y faces, qy dims (h+1, w): dec_fluid.rs:255-290
-            const i64 y = i / w, x = i - y * w;
-            const i64 yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
+            const I y = i / w, x = i - y * w;
+            const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
             const T velx = div_rn(add_rn(add_rn(add_rn(vx[yc * wx + x], vx[yc * wx + x + 1]), vx[ym * wx + x]),
                                          vx[ym * wx + x + 1]),
                                   T(4));
             const T vely = vy[y * w + x];
             const T ppx = back(add_rn((T)x, T(0.5)), ndt, velx);
             const T ppy = back(add_rn((T)y, T(0)), ndt, vely);
-            i64 x0, x1, y0, y1;
+            I x0, x1, y0, y1;
             T s, t;
             face_coord(ppx, T(0.5), w, x0, x1, s);
             face_coord(ppy, T(0), h + 1, y0, y1, t);
@@ -138,10 +142,10 @@ __global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, 
 }
 
 // Trilinear face sample of a part with dims (nz, ny, nx).
-template <class T>
-__device__ __forceinline__ T sample_part(const T* __restrict__ q, i64 nz, i64 ny, i64 nx, T ppx, T ox, T ppy, T oy,
+template <class T, class I>
+__device__ __forceinline__ T sample_part(const T* __restrict__ q, I nz, I ny, I nx, T ppx, T ox, T ppy, T oy,
                                          T ppz, T oz) {
-    i64 x0, x1, y0, y1, z0, z1;
+    I x0, x1, y0, y1, z0, z1;
     T s, t, u;
     face_coord(ppx, ox, nx, x0, x1, s);
     face_coord(ppy, oy, ny, y0, y1, t);
@@ -158,42 +162,45 @@ template <class T> __device__ __forceinline__ T avg4(T a, T b, T c, T d) {
 }
 
 // advect_mac, 3D extension
-template <class T>
+template <class T, class I>
 __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, Dims D,
                                 T ndt) {
-    const i64 d = D.d, h = D.h, w = D.w;
-    const i64 nz = D.nfz(), ny = D.nfy(), nf = D.nf();
+    const I d = (I)D.d, h = (I)D.h, w = (I)D.w;
+    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
+    auto FX = [&](I z, I y, I x) { return nz + ny + (z * h + y) * (w + 1) + x; };
+    auto FY = [&](I z, I y, I x) { return nz + (z * (h + 1) + y) * w + x; };
+    auto FZ = [&](I z, I y, I x) { return (z * h + y) * w + x; };
     const T* qz = src;
     const T* qy = src + nz;
     const T* qx = src + nz + ny;
     GRID_STRIDE(i, nf) {
         if (i >= nz + ny) {  // x faces (d, h, w+1)
-            const i64 j = i - nz - ny;
-            const i64 zy = j / (w + 1), x = j - zy * (w + 1);
-            const i64 z = zy / h, y = zy - z * h;
-            const i64 xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
+            const I j = i - nz - ny;
+            const I zy = j / (w + 1), x = j - zy * (w + 1);
+            const I z = zy / h, y = zy - z * h;
+            const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
             const T vx_ = vel[i];
-            const T vy_ = avg4(vel[D.fy(z, y, xc)], vel[D.fy(z, y + 1, xc)], vel[D.fy(z, y, xm)], vel[D.fy(z, y + 1, xm)]);
-            const T vz_ = avg4(vel[D.fz(z, y, xc)], vel[D.fz(z + 1, y, xc)], vel[D.fz(z, y, xm)], vel[D.fz(z + 1, y, xm)]);
+            const T vy_ = avg4(vel[FY(z, y, xc)], vel[FY(z, y + 1, xc)], vel[FY(z, y, xm)], vel[FY(z, y + 1, xm)]);
+            const T vz_ = avg4(vel[FZ(z, y, xc)], vel[FZ(z + 1, y, xc)], vel[FZ(z, y, xm)], vel[FZ(z + 1, y, xm)]);
             dst[i] = sample_part(qx, d, h, w + 1, back(add_rn((T)x, T(0)), ndt, vx_), T(0),
                                  back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0.5)), ndt, vz_),
                                  T(0.5));
         } else if (i >= nz) {  // y faces (d, h+1, w)
-            const i64 j = i - nz;
-            const i64 zy = j / w, x = j - zy * w;
-            const i64 z = zy / (h + 1), y = zy - z * (h + 1);
-            const i64 yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
-            const T vx_ = avg4(vel[D.fx(z, yc, x)], vel[D.fx(z, yc, x + 1)], vel[D.fx(z, ym, x)], vel[D.fx(z, ym, x + 1)]);
+            const I j = i - nz;
+            const I zy = j / w, x = j - zy * w;
+            const I z = zy / (h + 1), y = zy - z * (h + 1);
+            const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
+            const T vx_ = avg4(vel[FX(z, yc, x)], vel[FX(z, yc, x + 1)], vel[FX(z, ym, x)], vel[FX(z, ym, x + 1)]);
             const T vy_ = vel[i];
-            const T vz_ = avg4(vel[D.fz(z, yc, x)], vel[D.fz(z + 1, yc, x)], vel[D.fz(z, ym, x)], vel[D.fz(z + 1, ym, x)]);
+            const T vz_ = avg4(vel[FZ(z, yc, x)], vel[FZ(z + 1, yc, x)], vel[FZ(z, ym, x)], vel[FZ(z + 1, ym, x)]);
             dst[i] = sample_part(qy, d, h + 1, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
                                  back(add_rn((T)y, T(0)), ndt, vy_), T(0), back(add_rn((T)z, T(0.5)), ndt, vz_), T(0.5));
         } else {  // z faces (d+1, h, w)
-            const i64 zy = i / w, x = i - zy * w;
-            const i64 z = zy / h, y = zy - z * h;
-            const i64 zc = z < d - 1 ? z : d - 1, zm = z > 0 ? z - 1 : 0;
-            const T vx_ = avg4(vel[D.fx(zc, y, x)], vel[D.fx(zc, y, x + 1)], vel[D.fx(zm, y, x)], vel[D.fx(zm, y, x + 1)]);
-            const T vy_ = avg4(vel[D.fy(zc, y, x)], vel[D.fy(zc, y + 1, x)], vel[D.fy(zm, y, x)], vel[D.fy(zm, y + 1, x)]);
+            const I zy = i / w, x = i - zy * w;
+            const I z = zy / h, y = zy - z * h;
+            const I zc = z < d - 1 ? z : d - 1, zm = z > 0 ? z - 1 : 0;
+            const T vx_ = avg4(vel[FX(zc, y, x)], vel[FX(zc, y, x + 1)], vel[FX(zm, y, x)], vel[FX(zm, y, x + 1)]);
+            const T vy_ = avg4(vel[FY(zc, y, x)], vel[FY(zc, y + 1, x)], vel[FY(zm, y, x)], vel[FY(zm, y + 1, x)]);
             const T vz_ = vel[i];
             dst[i] = sample_part(qz, d + 1, h, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
                                  back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0)), ndt, vz_), T(0));
@@ -208,10 +215,18 @@ template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, dou
     const T ndt = -(T)dt;
     const T hix = (T)((double)D.w - 1.00001), hiy = (T)((double)D.h - 1.00001), hiz = (T)((double)D.d - 1.00001);
     const int nb = grid_blocks(g, D.nc(), kThreads);
-    if (D.nd == 2)
-        PG_LAUNCH(KK_ADVECT, g->stream, k_advect_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt, hix, hiy));
-    else
-        PG_LAUNCH(KK_ADVECT, g->stream, k_advect_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt, hix, hiy, hiz));
+    cudaStream_t s = g->stream;
+    if (D.nf() < ((i64)1 << 31)) {
+        if (D.nd == 2)
+            PG_LAUNCH(KK_ADVECT, s, k_advect_2d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, (int)D.h, (int)D.w, ndt, hix, hiy));
+        else
+            PG_LAUNCH(KK_ADVECT, s, k_advect_3d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, hix, hiy, hiz));
+    } else {
+        if (D.nd == 2)
+            PG_LAUNCH(KK_ADVECT, s, k_advect_2d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D.h, D.w, ndt, hix, hiy));
+        else
+            PG_LAUNCH(KK_ADVECT, s, k_advect_3d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, hix, hiy, hiz));
+    }
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -220,10 +235,18 @@ template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src,
     const Dims& D = g->dims;
     const T ndt = -(T)dt;
     const int nb = grid_blocks(g, D.nf(), kThreads);
-    if (D.nd == 2)
-        PG_LAUNCH(KK_ADVECT_MAC, g->stream, k_advect_mac_2d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D.h, D.w, ndt));
-    else
-        PG_LAUNCH(KK_ADVECT_MAC, g->stream, k_advect_mac_3d<T><<<nb, kThreads, 0, g->stream>>>(dst, src, vel, D, ndt));
+    cudaStream_t s = g->stream;
+    if (D.nf() < ((i64)1 << 31)) {
+        if (D.nd == 2)
+            PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_2d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, (int)D.h, (int)D.w, ndt));
+        else
+            PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_3d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt));
+    } else {
+        if (D.nd == 2)
+            PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_2d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D.h, D.w, ndt));
+        else
+            PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_3d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt));
+    }
     PG_CHECK_LAUNCH();
     return PG_OK;
 }

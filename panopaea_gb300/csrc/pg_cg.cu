@@ -103,10 +103,15 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
 // Fused search-direction update and operator application.
 template <class T, int ND, int PM>
 __global__ void __launch_bounds__(kCgThreads)
-    k_cg_spmv(const T* __restrict__ r, const T* __restrict__ zb, const T* __restrict__ p_old, T* __restrict__ p_new,
-              T* __restrict__ ap, const uint8_t* __restrict__ flags, Dims D, T dt, CgState* st, double* partials) {
+    k_cg_spmv(const T* __restrict__ r, const T* __restrict__ zb, T* p0, T* p1, T* __restrict__ ap,
+              const uint8_t* __restrict__ flags, Dims D, T dt, CgState* st, double* partials) {
     if (st->done) return;
     __shared__ double sm[32];
+    // Ping-pong by the device-side iteration count: iteration k reads
+    // p[k & 1] and writes p[(k + 1) & 1] (so a CUDA graph can replay it).
+    const i64 k = *(volatile const i64*)&st->iter;
+    const T* __restrict__ p_old = (k & 1) ? p1 : p0;
+    T* __restrict__ p_new = (k & 1) ? p0 : p1;
     const int first = st->first;
     const T beta = first ? T(0) : (T)st->beta;
     const i64 n = D.nc(), w = D.w, hw = D.h * D.w;
@@ -155,10 +160,14 @@ __global__ void __launch_bounds__(kCgThreads)
 
 template <class T, int PM>
 __global__ void __launch_bounds__(kCgThreads)
-    k_cg_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ ap,
+    k_cg_update(T* __restrict__ x, T* __restrict__ r, const T* p0, const T* p1, const T* __restrict__ ap,
                 const uint8_t* __restrict__ flags, i64 n, T dt, CgState* st, double* partials) {
     if (st->done) return;
     __shared__ double sm[32];
+    // The SpMV of this iteration wrote p[(iter + 1) & 1]; the last block
+    // increments iter only after every block has read it here.
+    const i64 k = *(volatile const i64*)&st->iter;
+    const T* __restrict__ p = ((k + 1) & 1) ? p1 : p0;
     const T alpha = (T)st->alpha, nalpha = -alpha;
     T rm = T(0);
     Acc<T> rz;
@@ -214,23 +223,116 @@ __global__ void k_cg_tail(const T* __restrict__ r, const T* __restrict__ p, T* _
 }
 
 template <class T, int PM>
-static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, i64 k, T dt, int nb, ZHook* hook) {
+static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* hook) {
     const Dims& D = g->dims;
-    T* p_old = buf.p[k & 1];
-    T* p_new = buf.p[(k + 1) & 1];
     cudaStream_t s = g->stream;
     if (D.nd == 2)
         PG_LAUNCH(KK_CG_SPMV, s,
-                  k_cg_spmv<T, 2, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, p_old, p_new, buf.ap, g->flags, D, dt,
-                                                                g->ws.state, g->ws.partials));
+                  k_cg_spmv<T, 2, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D,
+                                                                dt, g->ws.state, g->ws.partials));
     else
         PG_LAUNCH(KK_CG_SPMV, s,
-                  k_cg_spmv<T, 3, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, p_old, p_new, buf.ap, g->flags, D, dt,
-                                                                g->ws.state, g->ws.partials));
+                  k_cg_spmv<T, 3, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D,
+                                                                dt, g->ws.state, g->ws.partials));
     PG_LAUNCH(KK_CG_UPDATE, s,
-              k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, p_new, buf.ap, g->flags, D.nc(), dt,
-                                                           g->ws.state, g->ws.partials));
+              k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, D.nc(),
+                                                           dt, g->ws.state, g->ws.partials));
     if (PM == PM_ZBUF) hook->apply(g, buf.r, buf.z);
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-graph form of the iteration loop: a WHILE conditional node whose body
+// is one iteration (SpMV, update, the outer preconditioner's kernels) and a
+// one-thread kernel that clears the condition once the device-side stop
+// test has fired.  No host round trip and no launch past convergence.
+__global__ void k_cg_cond(const CgState* st, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, st->done ? 0u : 1u);
+}
+
+struct CgGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const void* key[8] = {};
+    double dt = 0.0;
+    int pm = -1, nd = 0;
+    uintptr_t hook_key = 0;
+    int body_kernels = 0;
+};
+
+struct CgGraphCache {
+    static constexpr int kSlots = 8;
+    CgGraph e[kSlots];
+    int next = 0;
+    ~CgGraphCache() {
+        for (auto& x : e) {
+            if (x.exec) cudaGraphExecDestroy(x.exec);
+            if (x.graph) cudaGraphDestroy(x.graph);
+        }
+    }
+};
+
+void release_cg_graphs(pg_grid* g) {
+    delete (CgGraphCache*)g->ws.graphs;
+    g->ws.graphs = nullptr;
+}
+
+template <class T, int PM>
+static int get_graph(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* hook, CgGraph** out) {
+    if (!g->ws.graphs) g->ws.graphs = new CgGraphCache();
+    CgGraphCache* C = (CgGraphCache*)g->ws.graphs;
+    const void* key[8] = {buf.x, buf.b, buf.r, buf.ap, buf.p[0], buf.p[1], buf.z, g->flags};
+    const uintptr_t hk = hook ? hook->key() : 0;
+    for (auto& e : C->e) {
+        if (e.exec && e.pm == PM && e.dt == (double)dt && e.nd == g->dims.nd && e.hook_key == hk &&
+            std::equal(key, key + 8, e.key)) {
+            *out = &e;
+            return PG_OK;
+        }
+    }
+    CgGraph& E = C->e[C->next];
+    C->next = (C->next + 1) % CgGraphCache::kSlots;
+    if (E.exec) cudaGraphExecDestroy(E.exec);
+    if (E.graph) cudaGraphDestroy(E.graph);
+    E = CgGraph();
+    PG_CUDA(cudaGraphCreate(&E.graph, 0));
+    cudaGraphConditionalHandle h;
+    PG_CUDA(cudaGraphConditionalHandleCreate(&h, E.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    PG_CUDA(cudaGraphAddNode(&node, E.graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t cs;
+    PG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaStream_t saved = g->stream;
+    g->stream = cs;
+    const int64_t before = prof_capture_begin();
+    cudaError_t err = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (err == cudaSuccess) {
+        launch_iter<T, PM>(g, buf, dt, nb, hook);
+        k_cg_cond<<<1, 1, 0, cs>>>(g->ws.state, h);
+        cudaGraph_t captured = nullptr;
+        err = cudaStreamEndCapture(cs, &captured);
+    }
+    E.body_kernels = (int)(prof_capture_end() - before) + 1;
+    g->stream = saved;
+    cudaStreamDestroy(cs);
+    if (err != cudaSuccess) {
+        cudaGraphDestroy(E.graph);
+        E = CgGraph();
+        return cuda_fail(err, "CG graph capture");
+    }
+    PG_CUDA(cudaGraphInstantiate(&E.exec, E.graph, 0));
+    std::copy(key, key + 8, E.key);
+    E.pm = PM;
+    E.dt = (double)dt;
+    E.nd = g->dims.nd;
+    E.hook_key = hk;
+    *out = &E;
+    return PG_OK;
 }
 
 template <class T, int PM>
@@ -250,7 +352,14 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
                                                          ws.partials));
     PG_CHECK_LAUNCH();
     if (PM == PM_ZBUF && (rc = hook->apply(g, buf.r, buf.z))) return rc;
-    // Poll interval: about 0.5 ms of device work per chunk.
+    // Device-side loop: one graph launch runs every iteration.
+    CgGraph* G = nullptr;
+    if (graphs_enabled() && cfg.max_iter > 0) {
+        if ((rc = get_graph<T, PM>(g, buf, dt, nb, hook, &G))) return rc;
+        PG_CUDA(cudaGraphLaunch(G->exec, s));
+    }
+    // Host-polled loop (profiling mode): chunks of about 0.5 ms of device
+    // work, two in flight; iterations past the stop test exit at entry.
     int chunk = cfg.check_every;
     if (chunk <= 0) {
         double us_per_iter = 4.0 + (double)n * 41.0 / 5.0e6;  // launch floor + HBM time
@@ -259,10 +368,10 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
     }
     i64 launched = 0;
     int slot = 0, pending = -1;
-    bool done = false;
+    bool done = G != nullptr;
     while (!done && launched < cfg.max_iter) {
         const i64 todo = std::min<i64>(chunk, cfg.max_iter - launched);
-        for (i64 k = 0; k < todo; ++k) launch_iter<T, PM>(g, buf, launched + k, dt, nb, hook);
+        for (i64 k = 0; k < todo; ++k) launch_iter<T, PM>(g, buf, dt, nb, hook);
         PG_CHECK_LAUNCH();
         launched += todo;
         PG_CUDA(cudaMemcpyAsync(ws.state_host + slot, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost, s));
@@ -277,6 +386,7 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
     PG_CUDA(cudaStreamSynchronize(s));
     CgState st;
     PG_CUDA(cudaMemcpy(&st, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost));
+    if (G) prof_add_launches((int64_t)G->body_kernels * std::max<i64>(st.iter, 1));
     if (stats) {
         stats->iterations = st.iter;
         stats->refinements = 0;

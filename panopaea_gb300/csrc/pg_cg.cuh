@@ -55,6 +55,8 @@ struct ZHook {
     // Enqueue z = M^-1 r on the grid's stream; must end with a kernel that
     // publishes z.r through cg_finish_rz.
     virtual int apply(pg_grid* g, const void* r, void* z) = 0;
+    // Identity of the kernel sequence apply() enqueues (graph cache key).
+    virtual uintptr_t key() const = 0;
     virtual ~ZHook() {}
 };
 

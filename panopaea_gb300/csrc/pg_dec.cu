@@ -11,6 +11,7 @@ namespace pg {
 constexpr int kThreads = 256;
 
 #define GRID_STRIDE(i, n) for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (i64)gridDim.x * blockDim.x)
+#define GRID_STRIDE_I(i, n) for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (I)gridDim.x * blockDim.x)
 
 // grid.rs:206-238: sign flip of one part of the face buffer.
 template <class T> __global__ void k_hodge1(T* __restrict__ out, const T* __restrict__ in, i64 n0, i64 n, int neg_first) {
@@ -26,11 +27,11 @@ template <class T> __global__ void k_copy(T* __restrict__ out, const T* __restri
 }
 
 // grid.rs:295-305: face = -bottom + top - left + right (2D).
-template <class T> __global__ void k_d1primal_2d(T* __restrict__ faces, const T* __restrict__ edges, i64 h, i64 w) {
+template <class T, class I> __global__ void k_d1primal_2d(T* __restrict__ faces, const T* __restrict__ edges, I h, I w) {
     const T* e0 = edges;
     const T* e1 = edges + (h + 1) * w;
-    GRID_STRIDE(i, h * w) {
-        const i64 y = i / w, x = i - y * w;
+    GRID_STRIDE_I(i, h * w) {
+        const I y = i / w, x = i - y * w;
         const T top = e0[y * w + x], bottom = e0[(y + 1) * w + x];
         const T left = e1[y * (w + 1) + x], right = e1[y * (w + 1) + x + 1];
         faces[i] = add_rn(sub_rn(add_rn(-bottom, top), left), right);
@@ -39,27 +40,27 @@ template <class T> __global__ void k_d1primal_2d(T* __restrict__ faces, const T*
 
 // grid.rs:318-334 and its 3D extension: interior faces get the negative
 // gradient, boundary faces are not written.
-template <class T> __global__ void k_d0dual(T* __restrict__ e, const T* __restrict__ p, Dims D) {
-    const i64 nz = D.nfz(), ny = D.nfy(), nf = D.nf();
-    const i64 h = D.h, w = D.w, hw = h * w;
-    GRID_STRIDE(i, nf) {
+template <class T, class I> __global__ void k_d0dual(T* __restrict__ e, const T* __restrict__ p, Dims D) {
+    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
+    const I h = D.h, w = D.w, hw = h * w;
+    GRID_STRIDE_I(i, nf) {
         if (i < nz) {  // vz faces (d+1, h, w)
-            const i64 z = i / hw, r = i - z * hw;
-            if (z == 0 || z == D.d) continue;
-            const i64 c = z * hw + r;
+            const I z = i / hw, r = i - z * hw;
+            if (z == 0 || z == (I)D.d) continue;
+            const I c = z * hw + r;
             e[i] = -sub_rn(p[c], p[c - hw]);
         } else if (i < nz + ny) {  // vy faces (d, h+1, w)
-            const i64 j = i - nz;
-            const i64 zy = j / w, x = j - zy * w;
-            const i64 z = zy / (h + 1), y = zy - z * (h + 1);
+            const I j = i - nz;
+            const I zy = j / w, x = j - zy * w;
+            const I z = zy / (h + 1), y = zy - z * (h + 1);
             if (y == 0 || y == h) continue;
-            const i64 c = (z * h + y) * w + x;
+            const I c = (z * h + y) * w + x;
             e[i] = -sub_rn(p[c], p[c - w]);
         } else {  // vx faces (d, h, w+1)
-            const i64 j = i - nz - ny;
-            const i64 zy = j / (w + 1), x = j - zy * (w + 1);
+            const I j = i - nz - ny;
+            const I zy = j / (w + 1), x = j - zy * (w + 1);
             if (x == 0 || x == w) continue;
-            const i64 c = zy * w + x;
+            const I c = zy * w + x;
             e[i] = sub_rn(p[c - 1], p[c]);
         }
     }
@@ -98,22 +99,22 @@ __global__ void k_laplacian(T* __restrict__ out, const T* __restrict__ p, const 
 // RHS of examples/dec_fluid.rs:68-83.  Interior faces are masked through the
 // cell's open bits; boundary faces through the per-face solid array (the
 // reference never masks them, and then face_solid is NULL).
-template <class T, int ND>
+template <class T, int ND, class I>
 __global__ void k_rhs(T* __restrict__ b, const T* __restrict__ vel, const uint8_t* __restrict__ flags,
                       const uint8_t* __restrict__ fsolid, Dims D) {
-    const i64 h = D.h, w = D.w;
-    GRID_STRIDE(c, D.nc()) {
-        const i64 zy = c / w, x = c - zy * w;
-        const i64 z = zy / h, y = zy - z * h;
+    const I h = D.h, w = D.w;
+    GRID_STRIDE_I(c, (I)D.nc()) {
+        const I zy = c / w, x = c - zy * w;
+        const I z = zy / h, y = zy - z * h;
         const uint8_t f = flags[c];
         // Is a face masked?  Interior faces: the cell's open bit; boundary
         // faces: the per-face solid array (NULL = never masked).
-        auto masked = [&](i64 idx, bool interior, uint8_t bit) -> bool {
+        auto masked = [&](I idx, bool interior, uint8_t bit) -> bool {
             if (interior) return !(f & bit);
             return fsolid != nullptr && fsolid[idx] != 0;
         };
-        const i64 iyl = D.fy(z, y, x), iyh = D.fy(z, y + 1, x);
-        const i64 ixl = D.fx(z, y, x), ixh = D.fx(z, y, x + 1);
+        const I iyl = (I)D.fy(z, y, x), iyh = (I)D.fy(z, y + 1, x);
+        const I ixl = (I)D.fx(z, y, x), ixh = (I)D.fx(z, y, x + 1);
         const bool myl = masked(iyl, y > 0, YLO), myh = masked(iyh, y < h - 1, YHI);
         const T ux_lo = masked(ixl, x > 0, XLO) ? T(0) : vel[ixl];
         const T ux_hi = masked(ixh, x < w - 1, XHI) ? T(0) : vel[ixh];
@@ -127,9 +128,9 @@ __global__ void k_rhs(T* __restrict__ b, const T* __restrict__ vel, const uint8_
         } else {
             const T uy_lo = myl ? T(0) : vel[iyl];
             const T uy_hi = myh ? T(0) : vel[iyh];
-            const i64 izl = D.fz(z, y, x), izh = D.fz(z + 1, y, x);
+            const I izl = (I)D.fz(z, y, x), izh = (I)D.fz(z + 1, y, x);
             const T uz_lo = masked(izl, z > 0, ZLO) ? T(0) : vel[izl];
-            const T uz_hi = masked(izh, z < D.d - 1, ZHI) ? T(0) : vel[izh];
+            const T uz_hi = masked(izh, z < (I)D.d - 1, ZHI) ? T(0) : vel[izh];
             v = add_rn(sub_rn(add_rn(sub_rn(sub_rn(uy_hi, uy_lo), ux_lo), ux_hi), uz_lo), uz_hi);
         }
         b[c] = -v;
@@ -141,33 +142,33 @@ __global__ void k_rhs(T* __restrict__ b, const T* __restrict__ vel, const uint8_
 // faces zeroed (walls).  zero_solid: solid interior faces zeroed after.
 // P is the pressure type: T (the reference's arithmetic), or double for a
 // float field projected with the FP64 pressure of the refined solve.
-template <class T, class P>
+template <class T, class P, class I>
 __global__ void k_project(T* __restrict__ vel, const P* __restrict__ p, const uint8_t* __restrict__ flags, Dims D, P dt,
                           int zero_solid) {
-    const i64 nz = D.nfz(), ny = D.nfy(), nf = D.nf();
-    const i64 h = D.h, w = D.w, hw = h * w;
-    GRID_STRIDE(i, nf) {
+    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
+    const I h = D.h, w = D.w, hw = h * w;
+    GRID_STRIDE_I(i, nf) {
         P e;
         bool open;
         if (i < nz) {
-            const i64 z = i / hw, r = i - z * hw;
-            if (z == 0 || z == D.d) { vel[i] = T(0); continue; }
-            const i64 c = z * hw + r;
+            const I z = i / hw, r = i - z * hw;
+            if (z == 0 || z == (I)D.d) { vel[i] = T(0); continue; }
+            const I c = z * hw + r;
             e = -sub_rn(p[c], p[c - hw]);
             open = flags[c] & ZLO;
         } else if (i < nz + ny) {
-            const i64 j = i - nz;
-            const i64 zy = j / w, x = j - zy * w;
-            const i64 z = zy / (h + 1), y = zy - z * (h + 1);
+            const I j = i - nz;
+            const I zy = j / w, x = j - zy * w;
+            const I z = zy / (h + 1), y = zy - z * (h + 1);
             if (y == 0 || y == h) { vel[i] = T(0); continue; }
-            const i64 c = (z * h + y) * w + x;
+            const I c = (z * h + y) * w + x;
             e = -sub_rn(p[c], p[c - w]);
             open = flags[c] & YLO;
         } else {
-            const i64 j = i - nz - ny;
-            const i64 zy = j / (w + 1), x = j - zy * (w + 1);
+            const I j = i - nz - ny;
+            const I zy = j / (w + 1), x = j - zy * (w + 1);
             if (x == 0 || x == w) { vel[i] = T(0); continue; }
-            const i64 c = zy * w + x;
+            const I c = zy * w + x;
             e = sub_rn(p[c - 1], p[c]);
             open = flags[c] & XLO;
         }
@@ -176,22 +177,22 @@ __global__ void k_project(T* __restrict__ vel, const P* __restrict__ p, const ui
 }
 
 // Wall step of examples/dec_fluid.rs:128-141 (3D: also vz at z = 0, d).
-template <class T> __global__ void k_walls(T* __restrict__ vel, Dims D) {
-    const i64 nz = D.nfz(), ny = D.nfy(), nf = D.nf();
-    const i64 h = D.h, w = D.w, hw = h * w;
-    GRID_STRIDE(i, nf) {
+template <class T, class I> __global__ void k_walls(T* __restrict__ vel, Dims D) {
+    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
+    const I h = D.h, w = D.w, hw = h * w;
+    GRID_STRIDE_I(i, nf) {
         bool wall;
         if (i < nz) {
-            const i64 z = i / hw;
-            wall = (z == 0 || z == D.d);
+            const I z = i / hw;
+            wall = (z == 0 || z == (I)D.d);
         } else if (i < nz + ny) {
-            const i64 j = i - nz;
-            const i64 zy = j / w;
-            const i64 y = zy % (h + 1);
+            const I j = i - nz;
+            const I zy = j / w;
+            const I y = zy % (h + 1);
             wall = (y == 0 || y == h);
         } else {
-            const i64 j = i - nz - ny;
-            const i64 x = j % (w + 1);
+            const I j = i - nz - ny;
+            const I x = j % (w + 1);
             wall = (x == 0 || x == w);
         }
         if (wall) vel[i] = T(0);
@@ -200,14 +201,14 @@ template <class T> __global__ void k_walls(T* __restrict__ vel, Dims D) {
 
 // Inflow box of examples/dec_fluid.rs:48-57: density = sd and the vy face
 // with the cell's index = sv, for cells in [lo, hi).
-template <class T>
-__global__ void k_source_box(T* __restrict__ rho, T* __restrict__ vel, Dims D, i64 z0, i64 y0, i64 x0, i64 bz, i64 by,
-                             i64 bx, T sd, T sv) {
-    GRID_STRIDE(i, bz * by * bx) {
-        const i64 zy = i / bx, x = x0 + (i - zy * bx);
-        const i64 z = z0 + zy / by, y = y0 + zy % by;
-        rho[D.cell(z, y, x)] = sd;
-        vel[D.fy(z, y, x)] = sv;
+template <class T, class I>
+__global__ void k_source_box(T* __restrict__ rho, T* __restrict__ vel, Dims D, I z0, I y0, I x0, I bz, I by,
+                             I bx, T sd, T sv) {
+    GRID_STRIDE_I(i, bz * by * bx) {
+        const I zy = i / bx, x = x0 + (i - zy * bx);
+        const I z = z0 + zy / by, y = y0 + zy % by;
+        rho[(I)D.cell(z, y, x)] = sd;
+        vel[(I)D.fy(z, y, x)] = sv;
     }
 }
 
@@ -217,14 +218,14 @@ template <class T> __global__ void k_source_field(T* __restrict__ rho, const T* 
 
 // Buoyancy (extension): vy = vy + coef * (0.5 * (rho[y-1] + rho[y])) on
 // interior y faces.
-template <class T> __global__ void k_buoyancy(T* __restrict__ vel, const T* __restrict__ rho, Dims D, T coef) {
-    const i64 h = D.h, w = D.w;
-    GRID_STRIDE(j, D.nfy()) {
-        const i64 zy = j / w, x = j - zy * w;
-        const i64 z = zy / (h + 1), y = zy - z * (h + 1);
+template <class T, class I> __global__ void k_buoyancy(T* __restrict__ vel, const T* __restrict__ rho, Dims D, T coef) {
+    const I h = D.h, w = D.w;
+    GRID_STRIDE_I(j, (I)D.nfy()) {
+        const I zy = j / w, x = j - zy * w;
+        const I z = zy / (h + 1), y = zy - z * (h + 1);
         if (y == 0 || y == h) continue;
-        const i64 c = (z * h + y) * w + x;
-        const i64 f = D.offy() + j;
+        const I c = (z * h + y) * w + x;
+        const I f = (I)D.offy() + j;
         vel[f] = add_rn(vel[f], mul_rn(coef, mul_rn(T(0.5), add_rn(rho[c - w], rho[c]))));
     }
 }
@@ -259,32 +260,87 @@ template <class T> int launch_laplacian(const pg_grid* g, T* out, const T* p, do
 template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel) {
     const Dims& D = g->dims;
     if (D.nd == 2)
-        PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 2><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D));
+        PG_IDX(g, PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 2, I><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D)));
     else
-        PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 3><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D));
+        PG_IDX(g, PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 3, I><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid) {
     const Dims& D = g->dims;
-    PG_LAUNCH(KK_PROJECT, g->stream, k_project<T, T><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, p, g->flags, D, (T)dt, zero_solid));
+    PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream, k_project<T, T, I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, p, g->flags, D, (T)dt, zero_solid)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid) {
     const Dims& D = g->dims;
-    PG_LAUNCH(KK_PROJECT, g->stream,
-              k_project<float, double><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
-                  vel, p, g->flags, D, dt, zero_solid));
+    PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream,
+              k_project<float, double, I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
+                  vel, p, g->flags, D, dt, zero_solid)));
+    PG_CHECK_LAUNCH();
+    return PG_OK;
+}
+
+// Projection with a double-float pressure p = ph + pl: the difference
+// p_lo - p_hi is formed exactly in the high parts (TwoSum), so the gradient
+// keeps its FP32 relative accuracy however large p is.
+__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) {
+    const float s = __fsub_rn(ah, bh);
+    const float bb = __fsub_rn(s, ah);
+    const float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(-bh, bb));
+    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(al, bl)));
+}
+
+template <class I>
+__global__ void k_project_df(float* __restrict__ vel, const float* __restrict__ ph, const float* __restrict__ pl,
+                             const uint8_t* __restrict__ flags, Dims D, float dt, int zero_solid) {
+    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
+    const I h = (I)D.h, w = (I)D.w, hw = h * w, d = (I)D.d;
+    GRID_STRIDE_I(i, nf) {
+        I lo, hi;
+        uint8_t bit;
+        if (i < nz) {
+            const I z = i / hw, r = i - z * hw;
+            if (z == 0 || z == d) { vel[i] = 0.f; continue; }
+            hi = z * hw + r;
+            lo = hi - hw;
+            bit = ZLO;
+        } else if (i < nz + ny) {
+            const I j = i - nz;
+            const I zy = j / w, x = j - zy * w;
+            const I z = zy / (h + 1), y = zy - z * (h + 1);
+            if (y == 0 || y == h) { vel[i] = 0.f; continue; }
+            hi = (z * h + y) * w + x;
+            lo = hi - w;
+            bit = YLO;
+        } else {
+            const I j = i - nz - ny;
+            const I zy = j / (w + 1), x = j - zy * (w + 1);
+            if (x == 0 || x == w) { vel[i] = 0.f; continue; }
+            hi = zy * w + x;
+            lo = hi - 1;
+            bit = XLO;
+        }
+        const bool open = flags[hi] & bit;
+        const float e = df_diff(ph[lo], pl[lo], ph[hi], pl[hi]);  // p_lo - p_hi = -grad p
+        vel[i] = (zero_solid && !open) ? 0.f : __fadd_rn(vel[i], __fmul_rn(dt, e));
+    }
+}
+
+int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid) {
+    const Dims& D = g->dims;
+    PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream,
+              k_project_df<I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
+                  vel, ph, pl, g->flags, D, (float)dt, zero_solid)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
 template <class T> int launch_walls(const pg_grid* g, T* vel) {
     const Dims& D = g->dims;
-    PG_LAUNCH(KK_DEC_OP, g->stream, k_walls<T><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, D));
+    PG_IDX(g, PG_LAUNCH(KK_DEC_OP, g->stream, k_walls<T, I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, D)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -301,9 +357,9 @@ template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const
     }
     const i64 n = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
     if (n == 0) return PG_OK;
-    PG_LAUNCH(KK_STEP_MISC, g->stream, k_source_box<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(
+    PG_IDX(g, PG_LAUNCH(KK_STEP_MISC, g->stream, k_source_box<T, I><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(
         rho, vel, D, lo[0], lo[1], lo[2], hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], (T)prm->source_density,
-        (T)prm->source_vy));
+        (T)prm->source_vy)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -317,7 +373,7 @@ template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* sr
 
 template <class T> int launch_buoyancy(const pg_grid* g, T* vel, const T* rho, double dt, double beta) {
     const Dims& D = g->dims;
-    PG_LAUNCH(KK_STEP_MISC, g->stream, k_buoyancy<T><<<grid_blocks(g, D.nfy(), kThreads), kThreads, 0, g->stream>>>(vel, rho, D, (T)(dt * beta)));
+    PG_IDX(g, PG_LAUNCH(KK_STEP_MISC, g->stream, k_buoyancy<T, I><<<grid_blocks(g, D.nfy(), kThreads), kThreads, 0, g->stream>>>(vel, rho, D, (T)(dt * beta))));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -361,15 +417,15 @@ using namespace pg;
         NEED(g && faces && edges, "pg_derivative_1_primal: NULL argument");                                 \
         NEED(g->dims.nd == 2, "pg_derivative_1_primal: 2D grids only");                                     \
         const i64 n = g->dims.nc();                                                                         \
-        PG_LAUNCH(KK_DEC_OP, g->stream, k_d1primal_2d<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(faces, edges, g->dims.h,  \
-                                                                                  g->dims.w));               \
+        PG_IDX(g, PG_LAUNCH(KK_DEC_OP, g->stream, k_d1primal_2d<T, I><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(faces, edges, g->dims.h,  \
+                                                                                  g->dims.w)));               \
         PG_CHECK_LAUNCH();                                                                                  \
         return PG_OK;                                                                                       \
     }                                                                                                       \
     extern "C" int pg_derivative_0_dual_##SFX(const pg_grid* g, T* edges, const T* faces) {                \
         NEED(g && faces && edges, "pg_derivative_0_dual: NULL argument");                                   \
         const i64 n = g->dims.nf();                                                                         \
-        PG_LAUNCH(KK_DEC_OP, g->stream, k_d0dual<T><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(edges, faces, g->dims));        \
+        PG_IDX(g, PG_LAUNCH(KK_DEC_OP, g->stream, k_d0dual<T, I><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(edges, faces, g->dims)));        \
         PG_CHECK_LAUNCH();                                                                                  \
         return PG_OK;                                                                                       \
     }                                                                                                       \

@@ -155,6 +155,7 @@ int pg_grid_destroy(pg_grid* g) {
     if (g->ws.ev[0]) cudaEventDestroy(g->ws.ev[0]);
     if (g->ws.ev[1]) cudaEventDestroy(g->ws.ev[1]);
     release_extras(g);
+    release_cg_graphs(g);
     delete g;
     return PG_OK;
 }

@@ -106,6 +106,7 @@ struct Workspace {
     void* vec = nullptr;         // extra CG vectors (lazily sized)
     size_t vec_bytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    void* graphs = nullptr;      // cached CG-loop graphs (pg_cg.cu)
 };
 
 constexpr int kMaxBlocks = 4096;
@@ -143,6 +144,19 @@ inline int bad_arg(const char* msg) {
     return PG_BAD_ARG;
 }
 
+// Index type for per-element kernels: 32-bit when every face index fits.
+inline bool idx32(const pg_grid* g) { return g->dims.nf() < ((i64)1 << 31); }
+#define PG_IDX(g, ...)              \
+    do {                            \
+        if (::pg::idx32(g)) {       \
+            typedef int I;          \
+            __VA_ARGS__;            \
+        } else {                    \
+            typedef ::pg::i64 I;    \
+            __VA_ARGS__;            \
+        }                           \
+    } while (0)
+
 // Blocks for a grid-stride kernel over n items.
 inline int grid_blocks(const pg_grid* g, i64 n, int threads, int per_sm = 8) {
     i64 b = (n + threads - 1) / threads;
@@ -161,6 +175,15 @@ enum KernelKind {
 };
 void prof_begin(cudaStream_t s, int kind);
 void prof_end(cudaStream_t s, int kind);
+// Stream capture into a graph: launches are counted separately (as graph
+// nodes) and get no timing events; graph executions add their kernels later.
+int64_t prof_capture_begin();
+int64_t prof_capture_end();
+void prof_add_launches(int64_t n);
+// Device-side graph loops are used unless per-kernel profiling is on or
+// PG_NO_GRAPHS=1 is set in the environment.
+bool graphs_enabled();
+void release_cg_graphs(pg_grid* g);
 
 // Every kernel launch of the library goes through this macro.
 #define PG_LAUNCH(kind, stream, ...)        \

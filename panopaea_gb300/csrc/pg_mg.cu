@@ -52,7 +52,13 @@ struct MgHierarchy {
     int nlev = 0;
     MgLevel lv[kMaxLevels];
     void* mem = nullptr;
+    uint64_t id = 0;  // unique per build (CUDA-graph cache key)
 };
+
+static uint64_t next_hierarchy_id() {
+    static uint64_t n = 0;
+    return ++n;
+}
 
 // Read-only view of one level for the kernels.
 struct LV {
@@ -333,6 +339,7 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
     release_mg(ex);
     if (g->dims.nc() >= (i64)1 << 31) return bad_arg("PG_PRECOND_MG: grid too large for 32-bit level indexing");
     MgHierarchy* H = new MgHierarchy();
+    H->id = next_hierarchy_id();
     H->D0 = g->dims;
     H->flags = g->flags;
     H->dt = dt;
@@ -501,6 +508,7 @@ struct MgHook : ZHook {
     MgHierarchy* H;
     int nsmooth;
     int apply(pg_grid* g, const void* r, void* z) override { return vcycle(g, *H, (const float*)r, (float*)z, nsmooth); }
+    uintptr_t key() const override { return (uintptr_t)(H->id << 8) | (uintptr_t)(nsmooth & 0xff); }
 };
 
 template <class T>

@@ -1,5 +1,6 @@
 // pg_prof.cu -- launch counting and per-kernel CUDA-event timing.
 #include <atomic>
+#include <cstdlib>
 #include <deque>
 #include <mutex>
 #include <vector>
@@ -16,6 +17,8 @@ static const char* kKindNames[KK_COUNT] = {
 
 namespace {
 std::atomic<int64_t> g_launches{0};
+thread_local bool t_capturing = false;
+thread_local int64_t t_captured = 0;
 
 struct Pending {
     cudaEvent_t a, b;
@@ -70,6 +73,10 @@ void drain(Prof& p, bool wait) {
 }  // namespace
 
 void prof_begin(cudaStream_t s, int kind) {
+    if (t_capturing) {
+        ++t_captured;
+        return;
+    }
     g_launches.fetch_add(1, std::memory_order_relaxed);
     Prof& p = prof();
     if (!p.on) return;
@@ -81,7 +88,7 @@ void prof_begin(cudaStream_t s, int kind) {
 
 void prof_end(cudaStream_t s, int kind) {
     Prof& p = prof();
-    if (!p.on) return;
+    if (!p.on || t_capturing) return;
     std::lock_guard<std::mutex> lk(p.m);
     if (!p.open[kind]) return;
     cudaEvent_t e = take(p);
@@ -89,6 +96,26 @@ void prof_end(cudaStream_t s, int kind) {
     p.pending.push_back(Pending{p.open[kind], e, kind});
     p.open[kind] = nullptr;
     if (p.pending.size() > 8192) drain(p, false);
+}
+
+int64_t prof_capture_begin() {
+    t_capturing = true;
+    return t_captured;
+}
+
+int64_t prof_capture_end() {
+    t_capturing = false;
+    return t_captured;
+}
+
+void prof_add_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+bool graphs_enabled() {
+    static const bool env_off = [] {
+        const char* v = getenv("PG_NO_GRAPHS");
+        return v && v[0] && v[0] != '0';
+    }();
+    return !env_off && !prof().on;
 }
 
 }  // namespace pg

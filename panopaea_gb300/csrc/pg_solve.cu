@@ -13,6 +13,7 @@ template <class T> int launch_copy(const pg_grid* g, T* out, const T* in, i64 n)
 template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel);
 template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid);
 int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid);
+int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid);
 template <class T> int launch_walls(const pg_grid* g, T* vel);
 template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const pg_step_params* prm);
 template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* src);
@@ -106,17 +107,112 @@ __global__ void k_x64_store(float* __restrict__ out, const double* __restrict__ 
         out[c] = (float)x[c];
 }
 
-// One FP64-residual evaluation; returns ||b - A x||inf on the host.
-static int residual64(pg_grid* g, const float* b, const double* x, double dt, float* r, double* rmax_host) {
+// ---------------------------------------------------------------------------
+// The same three operations in double-float: x = xh + xl held as two FP32
+// arrays (|xl| <= ulp(xh)/2), error-free transformations on the FP32 pipes
+// (TwoSum, TwoProduct by fma).  The differences x_c - x_nb, where the
+// refinement's cancellation happens, are formed exactly in the high parts.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kThreads)
+    k_residual_df(const float* __restrict__ b, const float* __restrict__ xh, const float* __restrict__ xl,
+                  const uint8_t* __restrict__ flags, Dims D, float dt, float* __restrict__ r, double* partials,
+                  unsigned int* counter, double* out) {
+    __shared__ double sm[32];
+    const i64 n = D.nc(), w = D.w, hw = D.h * D.w;
+    float m = 0.f;
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
+        const uint8_t f = flags[c];
+        const float hc = xh[c], lc = xl[c];
+        float sh = 0.f, sl = 0.f;  // sum over open faces of (x_c - x_nb)
+        auto face = [&](i64 k) {
+            float dh, de, t, te;
+            two_sum(hc, -xh[k], dh, de);
+            two_sum(sh, dh, t, te);
+            sh = t;
+            sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(te, de), __fsub_rn(lc, xl[k])));
+        };
+        if (f & XLO) face(c - 1);
+        if (f & XHI) face(c + 1);
+        if (f & YLO) face(c - w);
+        if (f & YHI) face(c + w);
+        if (ND == 3) {
+            if (f & ZLO) face(c - hw);
+            if (f & ZHI) face(c + hw);
+        }
+        const float ph = __fmul_rn(dt, sh);
+        const float pl = __fadd_rn(__fmaf_rn(dt, sh, -ph), __fmul_rn(dt, sl));  // dt * (sh + sl) - ph
+        float rh, re;
+        two_sum(b[c], -ph, rh, re);
+        const float rv = __fadd_rn(rh, __fsub_rn(re, pl));
+        r[c] = rv;
+        m = fmaxf(m, fabsf(rv));
+        if (rv != rv) m = __int_as_float(0x7f800000);  // NaN reported as inf
+    }
+    const double bm = block_max<kThreads>((double)m, sm);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bm;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v = fmax(v, __ldcg(partials + i));
+    v = block_max<kThreads>(v, sm);
+    if (threadIdx.x == 0) {
+        *out = v;
+        *counter = 0;
+    }
+}
+
+// (xh, xl) += d, renormalised.
+__global__ void k_xdf_add(float* __restrict__ xh, float* __restrict__ xl, const float* __restrict__ d, i64 n) {
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
+        float s, e;
+        two_sum(xh[c], d[c], s, e);
+        const float lo = __fadd_rn(xl[c], e);
+        const float h2 = __fadd_rn(s, lo);
+        xh[c] = h2;
+        xl[c] = __fsub_rn(lo, __fsub_rn(h2, s));
+    }
+}
+
+__global__ void k_xdf_store(float* __restrict__ out, const float* __restrict__ xh, const float* __restrict__ xl, i64 n) {
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x)
+        out[c] = __fadd_rn(xh[c], xl[c]);
+}
+
+// One FP64-class residual evaluation; returns ||b - A x||inf on the host.
+// x64 is a double array (native) or the [xh | xl] pair (double-float).
+static int residual64(pg_grid* g, const float* b, const void* x64, bool native, double dt, float* r,
+                      double* rmax_host) {
     Extras* ex = extras_of(g);
     const Dims& D = g->dims;
     const int nb = grid_blocks(g, D.nc(), kThreads, 8);
     double* dev_out = (double*)ex->small;
     unsigned int* counter = (unsigned int*)(dev_out + 1);
-    if (D.nd == 2)
-        PG_LAUNCH(KK_RESIDUAL64, g->stream, k_residual64<2><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
-    else
-        PG_LAUNCH(KK_RESIDUAL64, g->stream, k_residual64<3><<<nb, kThreads, 0, g->stream>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
+    cudaStream_t s = g->stream;
+    const double* x = (const double*)x64;
+    const float* xh = (const float*)x64;
+    const float* xl = xh + D.nc();
+    if (native) {
+        if (D.nd == 2)
+            PG_LAUNCH(KK_RESIDUAL64, s, k_residual64<2><<<nb, kThreads, 0, s>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
+        else
+            PG_LAUNCH(KK_RESIDUAL64, s, k_residual64<3><<<nb, kThreads, 0, s>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
+    } else {
+        if (D.nd == 2)
+            PG_LAUNCH(KK_RESIDUAL64, s, k_residual_df<2><<<nb, kThreads, 0, s>>>(b, xh, xl, g->flags, D, (float)dt, r, g->ws.partials, counter, dev_out));
+        else
+            PG_LAUNCH(KK_RESIDUAL64, s, k_residual_df<3><<<nb, kThreads, 0, s>>>(b, xh, xl, g->flags, D, (float)dt, r, g->ws.partials, counter, dev_out));
+    }
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaMemcpyAsync(rmax_host, dev_out, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
     PG_CUDA(cudaStreamSynchronize(g->stream));
@@ -165,8 +261,11 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     if ((rc = ex->buffer(Extras::kRin, 4 * n, &rin))) return rc;
     PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
     const int nb = grid_blocks(g, n, kThreads, 8);
+    const bool native = prm->fp64_native != 0;
+    float* xh = (float*)x64;
+    float* xl = xh + n;
     double rmax = 0.0;
-    if ((rc = residual64(g, b, (const double*)x64, dt, (float*)rin, &rmax))) return rc;
+    if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
     const double bmax = rmax;  // x = 0: r = b exactly
     const double target = prm->rel_stop ? prm->rel_tol * bmax : prm->threshold;
     pg_pcg_stats out{};
@@ -194,9 +293,12 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
                 out.status = s.status;
                 break;
             }
-            PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
+            if (native)
+                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
+            else
+                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_add<<<nb, kThreads, 0, g->stream>>>(xh, xl, (const float*)d, n));
             PG_CHECK_LAUNCH();
-            if ((rc = residual64(g, b, (const double*)x64, dt, (float*)rin, &rmax))) return rc;
+            if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
             if (!std::isfinite(rmax)) {
                 out.status = PG_NAN_DETECTED;
                 break;
@@ -211,7 +313,10 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     } else {
         out.status = PG_OK;
     }
-    PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n));
+    if (native)
+        PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n));
+    else
+        PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_store<<<nb, kThreads, 0, g->stream>>>(x, xh, xl, n));
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(g->stream));
     out.iterations = iters;
@@ -266,8 +371,12 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure, pg_
     if (sizeof(T) == 4 && prm->solver.refine > 0) {
         void* x64;
         if ((rc = ex->buffer(Extras::kX64, sizeof(double) * nc, &x64))) return rc;
-        if ((rc = launch_project_p64(g, (float*)vel, (const double*)x64, dt, prm->zero_solid_after_project)))
-            return rc;
+        if (prm->solver.fp64_native)
+            rc = launch_project_p64(g, (float*)vel, (const double*)x64, dt, prm->zero_solid_after_project);
+        else
+            rc = launch_project_df(g, (float*)vel, (const float*)x64, (const float*)x64 + nc, dt,
+                                   prm->zero_solid_after_project);
+        if (rc) return rc;
     } else if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project))) {
         return rc;
     }

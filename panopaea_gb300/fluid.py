@@ -40,6 +40,7 @@ class SolverConfig:
     inner_rel_tol: float = 0.0
     mg_levels: int = 0
     mg_smooth: int = 0
+    fp64_native: bool = False
 
     def to_c(self):
         p = N.SolverParams()
@@ -53,6 +54,7 @@ class SolverConfig:
         p.inner_rel_tol = float(self.inner_rel_tol)
         p.mg_levels = int(self.mg_levels)
         p.mg_smooth = int(self.mg_smooth)
+        p.fp64_native = int(bool(self.fp64_native))
         return p
 
 
