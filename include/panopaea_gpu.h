@@ -227,6 +227,35 @@ int pg_pcg_f64(const pg_grid* grid, int precond, double* x, const double* b, int
                double threshold, double* residual, double* auxiliary, double* search, double dt,
                pg_pcg_stats* stats);
 
+/* Allocation-free PCG.  No counterpart in the reference.
+ *
+ * The same solve as pg_pcg_f32 for callers that cannot allocate device
+ * memory: code whose device memory is all owned by a host framework's pool
+ * or arena (an allocation hidden inside a library call would escape its
+ * accounting), and time-critical loops where cudaMalloc / cudaFree would
+ * synchronise the device.  It takes no pg_grid (creating one allocates):
+ * the grid is (nd, d, h, w) with d = 1 for nd = 2, and the geometry is
+ * either NULL (no obstacles: every interior face open) or a device array of
+ * one byte per cell of face-open bits (1 = x-low, 2 = x-high, 4 = y-low,
+ * 8 = y-high, 16 = z-low, 32 = z-high; set a bit iff that face is interior
+ * and not solid).  The caller passes every input and output, as in
+ * pg_pcg_f32; cuda_stream may be NULL (legacy default stream).
+ *
+ * Its scratch -- CG state, reduction partials, a second search-direction
+ * buffer, and the wall-only face bits -- is one fixed 5.1 MiB device array
+ * in the library (held by every GPU that loads the library until the
+ * process exits), so grids are limited to 1,048,576 cells; larger grids
+ * are rejected with PG_BAD_ARG.  The first call on each device looks the
+ * array's device address up (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Every call
+ * shares the array and overwrites what the previous call left there (the
+ * state is cleared at the start of each call), so calls that overlap on the
+ * GPU -- on different streams, or from different threads -- race.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine. */
+int pg_pcg_noalloc_f32(int32_t nd, int64_t d, int64_t h, int64_t w, const uint8_t* cell_flags, int precond,
+                       float* x, const float* b, int64_t max_iterations, double threshold, float* residual,
+                       float* auxiliary, float* search, double dt, void* cuda_stream, pg_pcg_stats* stats);
+
 /* Pressure solve A x = b with library-owned work vectors: the reference's
  * PCG (refine = 0), or FP32 CG inside FP64 residual refinement (refine >
  * 0), with the preconditioner of `params`.  x is overwritten (initial

@@ -112,6 +112,8 @@ _SIGS = {
     "pg_copy_h2d": (_I, [_P, _P, _P, C.c_size_t]),
     "pg_copy_d2h": (_I, [_P, _P, _P, C.c_size_t]),
     "pg_solve_pressure_f32": (_I, [_P, C.POINTER(SolverParams), _P, _P, _D, C.POINTER(PcgStats)]),
+    "pg_pcg_noalloc_f32": (_I, [C.c_int32, _I64, _I64, _I64, _P, _I, _P, _P, _I64, _D, _P, _P, _P, _D, _P,
+                                C.POINTER(PcgStats)]),
     "pg_kernel_launches": (_I64, []),
     "pg_profile_enable": (_I, [_I]),
     "pg_profile_reset": (_I, []),

@@ -469,3 +469,179 @@ extern "C" int pg_pcg_f64(const pg_grid* g, int precond, double* x, const double
                           pg_pcg_stats* stats) {
     return pg::pcg_abi<double>(g, precond, x, b, max_iter, threshold, residual, auxiliary, search, dt, stats);
 }
+
+// ===========================================================================
+// pg_pcg_noalloc_f32 -- the PCG above for callers that cannot allocate
+// device memory: code whose device memory is all owned by a host
+// framework's pool or arena (a cudaMalloc inside a library call would escape
+// its accounting), and time-critical loops where a cudaMalloc / cudaFree
+// would synchronise the device.  Its scratch -- the CG state, the per-block
+// reduction partials, the second search-direction buffer and, when the
+// caller passes no geometry, the wall-only face-open bits -- lives in one
+// file-scope device array of fixed size instead of library allocations.
+#include <mutex>
+
+namespace pg {
+namespace noalloc {
+
+constexpr i64 kMaxCells = (i64)1 << 20;  // 1,048,576 cells (e.g. 1024^2, 101^3)
+constexpr size_t kStateBytes = 256;
+constexpr size_t kPartialBytes = sizeof(double) * 4 * kMaxBlocks;  // 128 KiB
+constexpr size_t kSearchBytes = sizeof(float) * kMaxCells;         // 4 MiB
+constexpr size_t kFlagBytes = kMaxCells;                           // 1 MiB
+constexpr size_t kBytes = kStateBytes + kPartialBytes + kSearchBytes + kFlagBytes;
+static_assert(sizeof(CgState) <= kStateBytes, "CgState must fit the scratch header");
+static_assert((kStateBytes + kPartialBytes) % 256 == 0, "search buffer alignment");
+
+// Held by every GPU that loads the library, until the process exits.
+static __device__ __align__(256) unsigned char g_scratch[kBytes];
+
+// Device address of g_scratch, looked up once per device with that device
+// current (in host code the symbol is only a stand-in, not an address).
+static std::mutex g_mu;
+static unsigned char* g_addr[256];
+
+static int scratch_address(unsigned char** out) {
+    int dev = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return bad_arg("pg_pcg_noalloc_f32: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+        unsigned char* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(pg_pcg_noalloc_f32 scratch)");
+        g_addr[dev] = p;
+    }
+    *out = g_addr[dev];
+    return PG_OK;
+}
+
+// Face-open bits of a grid without obstacles: every interior face open.
+__global__ void k_wall_flags(uint8_t* __restrict__ flags, Dims D) {
+    const int d = (int)D.d, h = (int)D.h, w = (int)D.w;
+    const int n = d * h * w;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int zy = c / w, x = c - zy * w;
+        const int z = zy / h, y = zy - z * h;
+        uint8_t f = 0;
+        if (x > 0) f |= XLO;
+        if (x < w - 1) f |= XHI;
+        if (y > 0) f |= YLO;
+        if (y < h - 1) f |= YHI;
+        if (D.nd == 3) {
+            if (z > 0) f |= ZLO;
+            if (z < d - 1) f |= ZHI;
+        }
+        flags[c] = f;
+    }
+}
+
+template <int PM>
+static int run(const Dims& D, const uint8_t* flags, float* x, const float* b, i64 max_iter, double threshold,
+               float* residual, float* auxiliary, float* search, double dt, cudaStream_t s, CgState* st,
+               double* partials, float* pbuf, pg_pcg_stats* stats) {
+    int dev = 0, sms = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const i64 n = D.nc();
+    const int nb = (int)std::max<i64>(1, std::min<i64>({(n + kCgThreads - 1) / kCgThreads, (i64)sms * 8,
+                                                        (i64)kMaxBlocks}));
+    const float fdt = (float)dt;
+    float* p[2] = {pbuf, search};
+    int64_t launches = 0;
+    // The CG state and its last-block tickets must start at zero.
+    PG_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
+    k_cg_init<float, PM><<<nb, kCgThreads, 0, s>>>(x, residual, b, flags, n, fdt, threshold, 0.0, max_iter, 1, st,
+                                                   partials);
+    PG_CHECK_LAUNCH();
+    ++launches;
+    const double us_per_iter = 4.0 + (double)n * 41.0 / 5.0e6;
+    const int chunk = (int)std::min(64.0, std::max(2.0, 600.0 / us_per_iter));
+    CgState hs;
+    i64 done_launch = 0;
+    bool done = false;
+    while (!done && done_launch < max_iter) {
+        const i64 todo = std::min<i64>(chunk, max_iter - done_launch);
+        for (i64 k = 0; k < todo; ++k) {
+            if (D.nd == 2)
+                k_cg_spmv<float, 2, PM><<<nb, kCgThreads, 0, s>>>(residual, nullptr, p[0], p[1], auxiliary, flags, D,
+                                                                  fdt, st, partials);
+            else
+                k_cg_spmv<float, 3, PM><<<nb, kCgThreads, 0, s>>>(residual, nullptr, p[0], p[1], auxiliary, flags, D,
+                                                                  fdt, st, partials);
+            k_cg_update<float, PM><<<nb, kCgThreads, 0, s>>>(x, residual, p[0], p[1], auxiliary, flags, n, fdt, st,
+                                                             partials);
+        }
+        PG_CHECK_LAUNCH();
+        launches += 2 * todo;
+        done_launch += todo;
+        PG_CUDA(cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+        PG_CUDA(cudaStreamSynchronize(s));
+        done = hs.done != 0;
+    }
+    PG_CUDA(cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    // Work vectors end as the reference leaves them (pcg.rs:51-77).
+    const i64 it = hs.iter;
+    float* p_cur = p[it & 1];
+    if (it > 0 && hs.status == PG_NOT_CONVERGED && it >= max_iter) {
+        k_cg_tail<float, PM><<<nb, kCgThreads, 0, s>>>(residual, p_cur, auxiliary, search, flags, n, fdt, st);
+        PG_CHECK_LAUNCH();
+        ++launches;
+    } else if (it > 0 && p_cur != search) {
+        PG_CUDA(cudaMemcpyAsync(search, p_cur, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    }
+    PG_CUDA(cudaStreamSynchronize(s));
+    prof_add_launches(launches);
+    if (stats) {
+        stats->iterations = hs.iter;
+        stats->refinements = 0;
+        stats->residual_max = hs.rmax;
+        stats->b_max = hs.bmax;
+        stats->threshold = hs.threshold;
+        stats->true_residual_max = -1.0;
+        stats->status = hs.status;
+    }
+    return hs.status;
+}
+
+}  // namespace noalloc
+}  // namespace pg
+
+extern "C" int pg_pcg_noalloc_f32(int32_t nd, int64_t d, int64_t h, int64_t w, const uint8_t* cell_flags,
+                                  int precond, float* x, const float* b, int64_t max_iterations, double threshold,
+                                  float* residual, float* auxiliary, float* search, double dt, void* cuda_stream,
+                                  pg_pcg_stats* stats) {
+    using namespace pg;
+    if (nd != 2 && nd != 3) return bad_arg("pg_pcg_noalloc_f32: nd must be 2 or 3");
+    if (nd == 2 && d != 1) return bad_arg("pg_pcg_noalloc_f32: 2D grids take d = 1");
+    if (d < 1 || h < 1 || w < 1) return bad_arg("pg_pcg_noalloc_f32: every dimension must be >= 1");
+    if (d > noalloc::kMaxCells / h / w || d * h * w > noalloc::kMaxCells)
+        return bad_arg("pg_pcg_noalloc_f32: grid larger than 1048576 cells, the size of its fixed scratch; "
+                       "use pg_pcg_f32");
+    if (!x || !b || !residual || !auxiliary || !search) return bad_arg("pg_pcg_noalloc_f32: NULL argument");
+    if (precond != PG_PRECOND_NONE && precond != PG_PRECOND_JACOBI)
+        return bad_arg("pg_pcg_noalloc_f32: precond must be PG_PRECOND_NONE or PG_PRECOND_JACOBI");
+    if (max_iterations < 0) return bad_arg("pg_pcg_noalloc_f32: max_iterations < 0");
+    unsigned char* base = nullptr;
+    int rc = noalloc::scratch_address(&base);
+    if (rc) return rc;
+    CgState* st = (CgState*)base;
+    double* partials = (double*)(base + noalloc::kStateBytes);
+    float* pbuf = (float*)(base + noalloc::kStateBytes + noalloc::kPartialBytes);
+    uint8_t* wflags = base + noalloc::kStateBytes + noalloc::kPartialBytes + noalloc::kSearchBytes;
+    const Dims D{nd, d, h, w};
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+    const uint8_t* flags = cell_flags;
+    if (!flags) {
+        noalloc::k_wall_flags<<<(int)std::min<i64>((D.nc() + 255) / 256, 1024), 256, 0, s>>>(wflags, D);
+        PG_CHECK_LAUNCH();
+        prof_add_launches(1);
+        flags = wflags;
+    }
+    if (precond == PG_PRECOND_JACOBI)
+        return noalloc::run<PM_JACOBI>(D, flags, x, b, max_iterations, threshold, residual, auxiliary, search, dt, s,
+                                       st, partials, pbuf, stats);
+    return noalloc::run<PM_NONE>(D, flags, x, b, max_iterations, threshold, residual, auxiliary, search, dt, s, st,
+                                 partials, pbuf, stats);
+}
