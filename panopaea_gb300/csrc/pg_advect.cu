@@ -173,11 +173,16 @@ __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, 
     const T* qz = src;
     const T* qy = src + nz;
     const T* qx = src + nz + ny;
-    GRID_STRIDE(i, nf) {
-        if (i >= nz + ny) {  // x faces (d, h, w+1)
-            const I j = i - nz - ny;
-            const I zy = j / (w + 1), x = j - zy * (w + 1);
-            const I z = zy / h, y = zy - z * h;
+    // One thread per index (z, y, x) of the (d+1) x (h+1) x (w+1) box: it
+    // computes the x, y and z faces that share that index, so the gathers of
+    // the three components hit the same cache lines (processing the three
+    // parts one after another re-reads each part from DRAM).
+    const I ex = w + 1, exy = (h + 1) * ex;
+    GRID_STRIDE(t, (d + 1) * exy) {
+        const I z = t / exy, r = t - z * exy;
+        const I y = r / ex, x = r - y * ex;
+        if (z < d && y < h) {  // x face (z, y, x), part dims (d, h, w+1)
+            const I i = FX(z, y, x);
             const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
             const T vx_ = vel[i];
             const T vy_ = avg4(vel[FY(z, y, xc)], vel[FY(z, y + 1, xc)], vel[FY(z, y, xm)], vel[FY(z, y + 1, xm)]);
@@ -185,19 +190,18 @@ __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, 
             dst[i] = sample_part(qx, d, h, w + 1, back(add_rn((T)x, T(0)), ndt, vx_), T(0),
                                  back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0.5)), ndt, vz_),
                                  T(0.5));
-        } else if (i >= nz) {  // y faces (d, h+1, w)
-            const I j = i - nz;
-            const I zy = j / w, x = j - zy * w;
-            const I z = zy / (h + 1), y = zy - z * (h + 1);
+        }
+        if (z < d && x < w) {  // y face (z, y, x), part dims (d, h+1, w)
+            const I i = FY(z, y, x);
             const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
             const T vx_ = avg4(vel[FX(z, yc, x)], vel[FX(z, yc, x + 1)], vel[FX(z, ym, x)], vel[FX(z, ym, x + 1)]);
             const T vy_ = vel[i];
             const T vz_ = avg4(vel[FZ(z, yc, x)], vel[FZ(z + 1, yc, x)], vel[FZ(z, ym, x)], vel[FZ(z + 1, ym, x)]);
             dst[i] = sample_part(qy, d, h + 1, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
                                  back(add_rn((T)y, T(0)), ndt, vy_), T(0), back(add_rn((T)z, T(0.5)), ndt, vz_), T(0.5));
-        } else {  // z faces (d+1, h, w)
-            const I zy = i / w, x = i - zy * w;
-            const I z = zy / h, y = zy - z * h;
+        }
+        if (y < h && x < w) {  // z face (z, y, x), part dims (d+1, h, w)
+            const I i = FZ(z, y, x);
             const I zc = z < d - 1 ? z : d - 1, zm = z > 0 ? z - 1 : 0;
             const T vx_ = avg4(vel[FX(zc, y, x)], vel[FX(zc, y, x + 1)], vel[FX(zm, y, x)], vel[FX(zm, y, x + 1)]);
             const T vy_ = avg4(vel[FY(zc, y, x)], vel[FY(zc, y + 1, x)], vel[FY(zm, y, x)], vel[FY(zm, y + 1, x)]);

@@ -158,6 +158,119 @@ __global__ void __launch_bounds__(kCgThreads)
     }
 }
 
+// The same fused SpMV for 3D grids as a z-marching 2.5D tile: a block owns
+// a 32 x 8 column tile and walks a chunk of z planes; each cell's inputs are
+// loaded once, its x/y neighbours come from a shared-memory plane tile (with
+// a one-cell halo the edge threads fill), its z neighbours from the
+// registers of the planes below and above.  Work items (tile, z chunk) are
+// handed out grid-stride, so the block count (and the reduction partials)
+// stays bounded for any grid size.  Same arithmetic as k_cg_spmv.
+constexpr int kTX = 32, kTY = 8;
+
+template <class T, int PM>
+__global__ void __launch_bounds__(kTX * kTY)
+    k_cg_spmv3t(const T* __restrict__ r, const T* __restrict__ zb, T* p0, T* p1, T* __restrict__ ap,
+                const uint8_t* __restrict__ flags, Dims D, T dt, CgState* st, double* partials, int tiles_x,
+                int tiles_y, int zc, int nwork) {
+    if (st->done) return;
+    __shared__ T S[kTY + 2][kTX + 2];
+    __shared__ double sm[32];
+    const i64 kit = *(volatile const i64*)&st->iter;
+    const T* __restrict__ p_old = (kit & 1) ? p1 : p0;
+    T* __restrict__ p_new = (kit & 1) ? p0 : p1;
+    const int first = st->first;
+    const T beta = first ? T(0) : (T)st->beta;
+    auto pn = [&](i64 k) -> T {
+        const T z = zval<T, PM>(r, flags, zb, k, dt);
+        return first ? z : z + beta * p_old[k];
+    };
+    const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+    const int w = (int)D.w, h = (int)D.h, d = (int)D.d;
+    const i64 hw = (i64)h * w;
+    const int per_plane = tiles_x * tiles_y;
+    Acc<T> acc;
+    for (int item = blockIdx.x; item < nwork; item += gridDim.x) {
+        const int tz = item / per_plane, t2 = item - tz * per_plane;
+        const int x = (t2 % tiles_x) * kTX + tx, y = (t2 / tiles_x) * kTY + ty;
+        const int z0 = tz * zc, z1 = min(z0 + zc, d);
+        const bool inside = x < w && y < h;
+        const i64 col = (i64)y * w + x;
+        T below = T(0), cur = T(0), above = T(0);
+        if (inside) {
+            if (z0 > 0) below = pn((i64)(z0 - 1) * hw + col);
+            cur = pn((i64)z0 * hw + col);
+        }
+        for (int z = z0; z < z1; ++z) {
+            const i64 c = (i64)z * hw + col;
+            if (inside && z + 1 < d) above = pn(c + hw);
+            S[ty + 1][tx + 1] = cur;
+            if (inside) {
+                if (tx == 0 && x > 0) S[ty + 1][0] = pn(c - 1);
+                if (tx == kTX - 1 && x + 1 < w) S[ty + 1][kTX + 1] = pn(c + 1);
+                if (ty == 0 && y > 0) S[0][tx + 1] = pn(c - w);
+                if (ty == kTY - 1 && y + 1 < h) S[kTY + 1][tx + 1] = pn(c + w);
+            }
+            __syncthreads();
+            if (inside) {
+                const uint8_t f = flags[c];
+                const T pc = cur;
+                const T gy_lo = (f & YLO) ? -sub_rn(pc, S[ty][tx + 1]) : T(0);
+                const T gy_hi = (f & YHI) ? -sub_rn(S[ty + 2][tx + 1], pc) : T(0);
+                const T gx_lo = (f & XLO) ? sub_rn(S[ty + 1][tx], pc) : T(0);
+                const T gx_hi = (f & XHI) ? sub_rn(pc, S[ty + 1][tx + 2]) : T(0);
+                T v = add_rn(sub_rn(sub_rn(gy_hi, gy_lo), gx_lo), gx_hi);
+                const T gz_lo = (f & ZLO) ? -sub_rn(pc, below) : T(0);
+                const T gz_hi = (f & ZHI) ? -sub_rn(above, pc) : T(0);
+                v = add_rn(sub_rn(v, gz_lo), gz_hi);
+                const T a = mul_rn(v, dt);
+                p_new[c] = pc;
+                ap[c] = a;
+                acc.add(pc * a);
+            }
+            __syncthreads();
+            below = cur;
+            cur = above;
+        }
+    }
+    const double s = block_sum<kTX * kTY>(acc.value(), sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    if (!last_block(&st->counter[1])) return;
+    const double pap = reduce_partials<false, kTX * kTY>(partials, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+        st->counter[1] = 0;
+        st->pap = pap;
+        if (!isfinite(pap)) {
+            st->status = PG_NAN_DETECTED;
+            st->done = 1;
+        } else if (!(pap > 0.0)) {
+            st->status = st->sigma == 0.0 ? PG_NOT_CONVERGED : PG_BREAKDOWN;
+            st->done = 1;
+        } else {
+            st->alpha = st->sigma / pap;  // pcg.rs:53
+        }
+    }
+}
+
+// Launch the fused SpMV: the 2.5D tile for 3D grids, the flat grid-stride
+// kernel for 2D.  Shared by every CG entry point.
+template <class T, int PM>
+static void spmv_launch(cudaStream_t s, int num_sms, const T* r, const T* zb, T* p0, T* p1, T* ap,
+                        const uint8_t* flags, const Dims& D, T dt, CgState* st, double* partials, int nb_flat) {
+    if (D.nd == 3) {
+        const int tiles_x = (int)((D.w + kTX - 1) / kTX), tiles_y = (int)((D.h + kTY - 1) / kTY);
+        const int cap = std::min(num_sms * 8, kMaxBlocks);
+        // about two work items per resident block, at least 4 planes each
+        const i64 want_chunks = std::max<i64>(1, (2 * (i64)cap + tiles_x * tiles_y - 1) / ((i64)tiles_x * tiles_y));
+        const int zc = (int)std::max<i64>(4, (D.d + want_chunks - 1) / want_chunks);
+        const int nwork = tiles_x * tiles_y * (int)((D.d + zc - 1) / zc);
+        const int nb = std::max(1, std::min(nwork, cap));
+        k_cg_spmv3t<T, PM><<<nb, kTX * kTY, 0, s>>>(r, zb, p0, p1, ap, flags, D, dt, st, partials, tiles_x, tiles_y,
+                                                    zc, nwork);
+    } else {
+        k_cg_spmv<T, 2, PM><<<nb_flat, kCgThreads, 0, s>>>(r, zb, p0, p1, ap, flags, D, dt, st, partials);
+    }
+}
+
 template <class T, int PM>
 __global__ void __launch_bounds__(kCgThreads)
     k_cg_update(T* __restrict__ x, T* __restrict__ r, const T* p0, const T* p1, const T* __restrict__ ap,
@@ -226,14 +339,9 @@ template <class T, int PM>
 static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* hook) {
     const Dims& D = g->dims;
     cudaStream_t s = g->stream;
-    if (D.nd == 2)
-        PG_LAUNCH(KK_CG_SPMV, s,
-                  k_cg_spmv<T, 2, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D,
-                                                                dt, g->ws.state, g->ws.partials));
-    else
-        PG_LAUNCH(KK_CG_SPMV, s,
-                  k_cg_spmv<T, 3, PM><<<nb, kCgThreads, 0, s>>>(buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D,
-                                                                dt, g->ws.state, g->ws.partials));
+    PG_LAUNCH(KK_CG_SPMV, s,
+              spmv_launch<T, PM>(s, g->num_sms, buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D, dt,
+                                 g->ws.state, g->ws.partials, nb));
     PG_LAUNCH(KK_CG_UPDATE, s,
               k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, D.nc(),
                                                            dt, g->ws.state, g->ws.partials));
@@ -563,12 +671,7 @@ static int run(const Dims& D, const uint8_t* flags, float* x, const float* b, i6
     while (!done && done_launch < max_iter) {
         const i64 todo = std::min<i64>(chunk, max_iter - done_launch);
         for (i64 k = 0; k < todo; ++k) {
-            if (D.nd == 2)
-                k_cg_spmv<float, 2, PM><<<nb, kCgThreads, 0, s>>>(residual, nullptr, p[0], p[1], auxiliary, flags, D,
-                                                                  fdt, st, partials);
-            else
-                k_cg_spmv<float, 3, PM><<<nb, kCgThreads, 0, s>>>(residual, nullptr, p[0], p[1], auxiliary, flags, D,
-                                                                  fdt, st, partials);
+            spmv_launch<float, PM>(s, sms, residual, nullptr, p[0], p[1], auxiliary, flags, D, fdt, st, partials, nb);
             k_cg_update<float, PM><<<nb, kCgThreads, 0, s>>>(x, residual, p[0], p[1], auxiliary, flags, n, fdt, st,
                                                              partials);
         }

@@ -177,25 +177,23 @@ __global__ void k_project(T* __restrict__ vel, const P* __restrict__ p, const ui
 }
 
 // Wall step of examples/dec_fluid.rs:128-141 (3D: also vz at z = 0, d).
+// Only the boundary faces are visited: 2dh x-walls, 2dw y-walls, 2hw z-walls.
 template <class T, class I> __global__ void k_walls(T* __restrict__ vel, Dims D) {
-    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
-    const I h = D.h, w = D.w, hw = h * w;
-    GRID_STRIDE_I(i, nf) {
-        bool wall;
-        if (i < nz) {
-            const I z = i / hw;
-            wall = (z == 0 || z == (I)D.d);
-        } else if (i < nz + ny) {
-            const I j = i - nz;
-            const I zy = j / w;
-            const I y = zy % (h + 1);
-            wall = (y == 0 || y == h);
-        } else {
-            const I j = i - nz - ny;
-            const I x = j % (w + 1);
-            wall = (x == 0 || x == w);
+    const I d = (I)D.d, h = (I)D.h, w = (I)D.w;
+    const I nx = 2 * d * h, ny = 2 * d * w, nz = D.nd == 3 ? 2 * h * w : 0;
+    const I offy = (I)D.offy(), offx = (I)D.offx();
+    GRID_STRIDE_I(i, nx + ny + nz) {
+        if (i < nx) {  // vx at x = 0 and x = w, rows (z, y)
+            const I row = i >> 1;
+            vel[offx + row * (w + 1) + ((i & 1) ? w : 0)] = T(0);
+        } else if (i < nx + ny) {  // vy at y = 0 and y = h, (z, x)
+            const I j = i - nx, side = j / (d * w), k = j - side * d * w;
+            const I z = k / w, x = k - z * w;
+            vel[offy + (z * (h + 1) + (side ? h : 0)) * w + x] = T(0);
+        } else {  // vz at z = 0 and z = d, (y, x)
+            const I j = i - nx - ny, side = j / (h * w), k = j - side * h * w;
+            vel[(side ? d : 0) * h * w + k] = T(0);
         }
-        if (wall) vel[i] = T(0);
     }
 }
 

@@ -172,6 +172,102 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// k_residual_df for 3D grids as a z-marching 2.5D tile (32 x 8 columns; x/y
+// neighbours from shared memory, z neighbours from registers), so each cell's
+// (xh, xl) is loaded once.  Same arithmetic as k_residual_df.
+constexpr int kRTX = 32, kRTY = 8;
+
+__global__ void __launch_bounds__(kRTX * kRTY)
+    k_residual_df3t(const float* __restrict__ b, const float* __restrict__ xh, const float* __restrict__ xl,
+                    const uint8_t* __restrict__ flags, Dims D, float dt, float* __restrict__ r, double* partials,
+                    unsigned int* counter, double* out, int tiles_x, int tiles_y, int zc, int nwork) {
+    __shared__ float SH[kRTY + 2][kRTX + 2], SL[kRTY + 2][kRTX + 2];
+    __shared__ double sm[32];
+    const int tx = threadIdx.x % kRTX, ty = threadIdx.x / kRTX;
+    const int w = (int)D.w, h = (int)D.h, d = (int)D.d;
+    const i64 hw = (i64)h * w;
+    const int per_plane = tiles_x * tiles_y;
+    float m = 0.f;
+    for (int item = blockIdx.x; item < nwork; item += gridDim.x) {
+        const int tz = item / per_plane, t2 = item - tz * per_plane;
+        const int x = (t2 % tiles_x) * kRTX + tx, y = (t2 / tiles_x) * kRTY + ty;
+        const int z0 = tz * zc, z1 = min(z0 + zc, d);
+        const bool inside = x < w && y < h;
+        const i64 col = (i64)y * w + x;
+        float bh = 0.f, bl = 0.f, ch = 0.f, cl = 0.f, ah = 0.f, al = 0.f;  // below / current / above
+        if (inside) {
+            if (z0 > 0) {
+                bh = xh[(i64)(z0 - 1) * hw + col];
+                bl = xl[(i64)(z0 - 1) * hw + col];
+            }
+            ch = xh[(i64)z0 * hw + col];
+            cl = xl[(i64)z0 * hw + col];
+        }
+        for (int z = z0; z < z1; ++z) {
+            const i64 c = (i64)z * hw + col;
+            if (inside && z + 1 < d) {
+                ah = xh[c + hw];
+                al = xl[c + hw];
+            }
+            SH[ty + 1][tx + 1] = ch;
+            SL[ty + 1][tx + 1] = cl;
+            if (inside) {
+                if (tx == 0 && x > 0) { SH[ty + 1][0] = xh[c - 1]; SL[ty + 1][0] = xl[c - 1]; }
+                if (tx == kRTX - 1 && x + 1 < w) { SH[ty + 1][kRTX + 1] = xh[c + 1]; SL[ty + 1][kRTX + 1] = xl[c + 1]; }
+                if (ty == 0 && y > 0) { SH[0][tx + 1] = xh[c - w]; SL[0][tx + 1] = xl[c - w]; }
+                if (ty == kRTY - 1 && y + 1 < h) { SH[kRTY + 1][tx + 1] = xh[c + w]; SL[kRTY + 1][tx + 1] = xl[c + w]; }
+            }
+            __syncthreads();
+            if (inside) {
+                const uint8_t f = flags[c];
+                float sh = 0.f, sl = 0.f;
+                auto face = [&](float nh, float nl) {
+                    float dh, de, t, te;
+                    two_sum(ch, -nh, dh, de);
+                    two_sum(sh, dh, t, te);
+                    sh = t;
+                    sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(te, de), __fsub_rn(cl, nl)));
+                };
+                if (f & XLO) face(SH[ty + 1][tx], SL[ty + 1][tx]);
+                if (f & XHI) face(SH[ty + 1][tx + 2], SL[ty + 1][tx + 2]);
+                if (f & YLO) face(SH[ty][tx + 1], SL[ty][tx + 1]);
+                if (f & YHI) face(SH[ty + 2][tx + 1], SL[ty + 2][tx + 1]);
+                if (f & ZLO) face(bh, bl);
+                if (f & ZHI) face(ah, al);
+                const float ph = __fmul_rn(dt, sh);
+                const float pl = __fadd_rn(__fmaf_rn(dt, sh, -ph), __fmul_rn(dt, sl));
+                float rh, re;
+                two_sum(b[c], -ph, rh, re);
+                const float rv = __fadd_rn(rh, __fsub_rn(re, pl));
+                r[c] = rv;
+                m = fmaxf(m, fabsf(rv));
+                if (rv != rv) m = __int_as_float(0x7f800000);
+            }
+            __syncthreads();
+            bh = ch;
+            bl = cl;
+            ch = ah;
+            cl = al;
+        }
+    }
+    const double bm = block_max<kRTX * kRTY>((double)m, sm);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bm;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v = fmax(v, __ldcg(partials + i));
+    v = block_max<kRTX * kRTY>(v, sm);
+    if (threadIdx.x == 0) {
+        *out = v;
+        *counter = 0;
+    }
+}
+
 // (xh, xl) += d, renormalised.
 __global__ void k_xdf_add(float* __restrict__ xh, float* __restrict__ xl, const float* __restrict__ d, i64 n) {
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
@@ -208,10 +304,19 @@ static int residual64(pg_grid* g, const float* b, const void* x64, bool native, 
         else
             PG_LAUNCH(KK_RESIDUAL64, s, k_residual64<3><<<nb, kThreads, 0, s>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
     } else {
-        if (D.nd == 2)
+        if (D.nd == 2) {
             PG_LAUNCH(KK_RESIDUAL64, s, k_residual_df<2><<<nb, kThreads, 0, s>>>(b, xh, xl, g->flags, D, (float)dt, r, g->ws.partials, counter, dev_out));
-        else
-            PG_LAUNCH(KK_RESIDUAL64, s, k_residual_df<3><<<nb, kThreads, 0, s>>>(b, xh, xl, g->flags, D, (float)dt, r, g->ws.partials, counter, dev_out));
+        } else {
+            const int tiles_x = (int)((D.w + kRTX - 1) / kRTX), tiles_y = (int)((D.h + kRTY - 1) / kRTY);
+            const int cap = std::min(g->num_sms * 8, kMaxBlocks);
+            const i64 want = std::max<i64>(1, (2 * (i64)cap + tiles_x * tiles_y - 1) / ((i64)tiles_x * tiles_y));
+            const int zc = (int)std::max<i64>(4, (D.d + want - 1) / want);
+            const int nwork = tiles_x * tiles_y * (int)((D.d + zc - 1) / zc);
+            const int nbt = std::max(1, std::min(nwork, cap));
+            PG_LAUNCH(KK_RESIDUAL64, s,
+                      k_residual_df3t<<<nbt, kRTX * kRTY, 0, s>>>(b, xh, xl, g->flags, D, (float)dt, r, g->ws.partials,
+                                                                  counter, dev_out, tiles_x, tiles_y, zc, nwork));
+        }
     }
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaMemcpyAsync(rmax_host, dev_out, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
@@ -264,55 +369,67 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     const bool native = prm->fp64_native != 0;
     float* xh = (float*)x64;
     float* xl = xh + n;
-    double rmax = 0.0;
-    if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
-    const double bmax = rmax;  // x = 0: r = b exactly
-    const double target = prm->rel_stop ? prm->rel_tol * bmax : prm->threshold;
+    double rmax = 0.0, bmax = 0.0, target = 0.0;
     pg_pcg_stats out{};
-    out.b_max = bmax;
-    out.threshold = target;
     out.status = PG_NOT_CONVERGED;
     i64 iters = 0;
     int rounds = 0;
-    if (!(bmax < target) && !(bmax == 0.0)) {
-        for (rounds = 0; rounds < prm->refine; ++rounds) {
-            // Inner tolerance: reach half the outer target, but never ask FP32
-            // CG for more than ~1e-5 relative per round.
-            double inner = prm->inner_rel_tol > 0 ? prm->inner_rel_tol : 0.5 * target / rmax;
-            inner = std::max(inner, 1e-5);
-            CgBuffers<float> buf{(float*)d, (const float*)rin, (float*)rr, (float*)ap, {(float*)p0, (float*)p1}};
-            CgConfig cfg{prm->precond, prm->max_iter, 0.0, std::min(inner, 0.5), dt, prm->check_every, 1};
-            pg_pcg_stats s{};
-            if (prm->precond == PG_PRECOND_MG)
-                rc = solve_mgpcg<float>(g, prm, cfg, buf, &s);
-            else
-                rc = run_cg<float>(g, cfg, buf, &s);
-            if (rc) return rc;
-            iters += s.iterations;
-            if (s.status == PG_NAN_DETECTED || s.status == PG_BREAKDOWN) {
-                out.status = s.status;
-                break;
-            }
-            if (native)
-                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
-            else
-                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_add<<<nb, kThreads, 0, g->stream>>>(xh, xl, (const float*)d, n));
-            PG_CHECK_LAUNCH();
-            if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
-            if (!std::isfinite(rmax)) {
-                out.status = PG_NAN_DETECTED;
-                break;
-            }
-            if (rmax <= target) {
-                out.status = PG_OK;
-                ++rounds;
-                break;
-            }
-            if (iters >= prm->max_iter * (i64)prm->refine) break;
+    while (rounds < prm->refine) {
+        // Round 0 solves A d = b itself (x = 0, so the residual is b exactly
+        // and no residual kernel is needed); later rounds solve for the
+        // correction of the FP64-class residual r = b - A x.
+        CgBuffers<float> buf{(float*)d, rounds == 0 ? b : (const float*)rin, (float*)rr, (float*)ap,
+                             {(float*)p0, (float*)p1}};
+        CgConfig cfg{prm->precond, prm->max_iter, 0.0, 0.0, dt, prm->check_every, 1};
+        if (rounds == 0 && !prm->rel_stop) {
+            cfg.threshold = 0.5 * prm->threshold;
+        } else {
+            // Reach half the outer target, but never ask FP32 CG for more
+            // than ~1e-5 relative per round.
+            double inner = prm->inner_rel_tol > 0 ? prm->inner_rel_tol
+                           : rounds == 0      ? 0.5 * prm->rel_tol
+                                              : 0.5 * target / rmax;
+            cfg.rel_tol = std::min(std::max(inner, 1e-5), 0.5);
         }
-    } else {
-        out.status = PG_OK;
+        pg_pcg_stats s{};
+        if (prm->precond == PG_PRECOND_MG)
+            rc = solve_mgpcg<float>(g, prm, cfg, buf, &s);
+        else
+            rc = run_cg<float>(g, cfg, buf, &s);
+        if (rc) return rc;
+        iters += s.iterations;
+        ++rounds;
+        if (rounds == 1) {
+            bmax = s.b_max;
+            target = prm->rel_stop ? prm->rel_tol * bmax : prm->threshold;
+            rmax = bmax;
+            if (bmax == 0.0) {  // x = 0 is exact
+                out.status = PG_OK;
+                break;
+            }
+        }
+        if (s.status == PG_NAN_DETECTED || s.status == PG_BREAKDOWN) {
+            out.status = s.status;
+            break;
+        }
+        if (native)
+            PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
+        else
+            PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_add<<<nb, kThreads, 0, g->stream>>>(xh, xl, (const float*)d, n));
+        PG_CHECK_LAUNCH();
+        if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
+        if (!std::isfinite(rmax)) {
+            out.status = PG_NAN_DETECTED;
+            break;
+        }
+        if (rmax <= target) {
+            out.status = PG_OK;
+            break;
+        }
+        if (iters >= prm->max_iter * (i64)prm->refine) break;
     }
+    out.b_max = bmax;
+    out.threshold = target;
     if (native)
         PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n));
     else
