@@ -199,10 +199,17 @@ __global__ void __launch_bounds__(kTX * kTY)
         if (inside) {
             if (z0 > 0) below = pn((i64)(z0 - 1) * hw + col);
             cur = pn((i64)z0 * hw + col);
+            if (z0 + 1 < d) above = pn((i64)(z0 + 1) * hw + col);
         }
         for (int z = z0; z < z1; ++z) {
             const i64 c = (i64)z * hw + col;
-            if (inside && z + 1 < d) above = pn(c + hw);
+            // Loads for plane z + 2 are issued here and combined only after
+            // this plane's stencil, so their latency overlaps the step.
+            T rz = T(0), rp = T(0);
+            if (inside && z + 2 < d && z + 1 < z1) {
+                rz = zval<T, PM>(r, flags, zb, c + 2 * hw, dt);
+                if (!first) rp = p_old[c + 2 * hw];
+            }
             S[ty + 1][tx + 1] = cur;
             if (inside) {
                 if (tx == 0 && x > 0) S[ty + 1][0] = pn(c - 1);
@@ -230,6 +237,7 @@ __global__ void __launch_bounds__(kTX * kTY)
             __syncthreads();
             below = cur;
             cur = above;
+            above = first ? rz : rz + beta * rp;
         }
     }
     const double s = block_sum<kTX * kTY>(acc.value(), sm);

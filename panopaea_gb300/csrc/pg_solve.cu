@@ -202,12 +202,18 @@ __global__ void __launch_bounds__(kRTX * kRTY)
             }
             ch = xh[(i64)z0 * hw + col];
             cl = xl[(i64)z0 * hw + col];
+            if (z0 + 1 < d) {
+                ah = xh[(i64)(z0 + 1) * hw + col];
+                al = xl[(i64)(z0 + 1) * hw + col];
+            }
         }
         for (int z = z0; z < z1; ++z) {
             const i64 c = (i64)z * hw + col;
-            if (inside && z + 1 < d) {
-                ah = xh[c + hw];
-                al = xl[c + hw];
+            // plane z + 2 is loaded one step ahead of its use
+            float nh = 0.f, nl = 0.f;
+            if (inside && z + 2 < d && z + 1 < z1) {
+                nh = xh[c + 2 * hw];
+                nl = xl[c + 2 * hw];
             }
             SH[ty + 1][tx + 1] = ch;
             SL[ty + 1][tx + 1] = cl;
@@ -248,6 +254,8 @@ __global__ void __launch_bounds__(kRTX * kRTY)
             bl = cl;
             ch = ah;
             cl = al;
+            ah = nh;
+            al = nl;
         }
     }
     const double bm = block_max<kRTX * kRTY>((double)m, sm);
