@@ -273,6 +273,36 @@ int pg_step_f64(const pg_grid* grid, const pg_step_params* params, double* vel, 
                 double* pressure, pg_pcg_stats* stats);
 
 /* ----------------------------------------------------------------------- */
+/* Batches of independent 2D grids (extension; the reference steps a single
+ * grid, examples/dec_fluid.rs:46-141).  Grids of different sizes are packed
+ * back to back: grid i's cell field starts at cell_offsets[i] and its face
+ * field at face_offsets[i], each in the reference layout.  Every stage of
+ * the step is one launch over all grids; each grid has its own CG scalars
+ * and stop rule, converged grids retire, the CG loop is a CUDA graph. */
+typedef struct pg_batch pg_batch;
+int pg_batch_create_2d(int32_t count, const int64_t* heights, const int64_t* widths, pg_batch** out);
+int pg_batch_destroy(pg_batch* batch);
+int pg_batch_set_stream(pg_batch* batch, void* cuda_stream);
+/* count + 1 offsets each (the last is the packed total). */
+int pg_batch_layout(const pg_batch* batch, int64_t* cell_offsets, int64_t* face_offsets);
+/* Packed host cell mask (1 = solid; a face is solid iff an adjacent cell is); NULL clears. */
+int pg_batch_set_solid_cells(pg_batch* batch, const uint8_t* host_cell_solid);
+/* Tile shape (tile_x * tile_y threads, a multiple of 32, <= 256) and whether
+ * the search-direction update is fused into the SpMV. */
+int pg_batch_tile(const pg_batch* batch, int32_t* tile_x, int32_t* tile_y, int32_t* fused);
+int pg_batch_set_tile(pg_batch* batch, int32_t tile_x, int32_t tile_y, int32_t fused);
+/* Time the candidate tile shapes and fusion choices on this batch and keep
+ * the fastest; with cache_path, reuse / append "key tx ty fused" lines
+ * keyed by device and batch shape. */
+int pg_batch_autotune(pg_batch* batch, const char* cache_path);
+/* One step of every grid.  params->source_enabled must be 0 (use
+ * source_field, a packed device cell field); solver: NONE or JACOBI, no
+ * refinement.  stats: count entries (may be NULL).  Returns PG_OK, or the
+ * first non-OK per-grid status. */
+int pg_batch_step_f32(pg_batch* batch, const pg_step_params* params, float* vel, float* density, float* pressure,
+                      pg_pcg_stats* stats);
+
+/* ----------------------------------------------------------------------- */
 /* Instrumentation (no reference counterpart; the reference only prints
  * wall-clock ms around the PCG, examples/dec_fluid.rs:87,121). */
 

@@ -6,6 +6,7 @@ reference's Rust API (grid/field types, DEC operators, PCG, advection, step).
 """
 
 from . import _native
+from .batch import Batch2d, partition_by_cost
 from .fluid import SolverConfig, StepConfig, advect, advect_mac, solve_pressure, step
 from .grid import Grid2d, Grid3d, Simplex1, Simplex2
 from .pcg import IDENTITY, JACOBI, LaplacianOperator, Preconditioner, precond_conjugate_gradient
@@ -13,6 +14,7 @@ from .pcg import IDENTITY, JACOBI, LaplacianOperator, Preconditioner, precond_co
 __all__ = [
     "Grid2d", "Grid3d", "Simplex1", "Simplex2", "IDENTITY", "JACOBI", "LaplacianOperator", "Preconditioner",
     "precond_conjugate_gradient", "advect", "advect_mac", "step", "solve_pressure", "StepConfig", "SolverConfig",
+    "Batch2d", "partition_by_cost",
 ]
 
 

@@ -114,6 +114,15 @@ _SIGS = {
     "pg_solve_pressure_f32": (_I, [_P, C.POINTER(SolverParams), _P, _P, _D, C.POINTER(PcgStats)]),
     "pg_pcg_noalloc_f32": (_I, [C.c_int32, _I64, _I64, _I64, _P, _I, _P, _P, _I64, _D, _P, _P, _P, _D, _P,
                                 C.POINTER(PcgStats)]),
+    "pg_batch_create_2d": (_I, [C.c_int32, _P, _P, C.POINTER(_P)]),
+    "pg_batch_destroy": (_I, [_P]),
+    "pg_batch_set_stream": (_I, [_P, _P]),
+    "pg_batch_layout": (_I, [_P, _P, _P]),
+    "pg_batch_set_solid_cells": (_I, [_P, _P]),
+    "pg_batch_tile": (_I, [_P, _P, _P, _P]),
+    "pg_batch_set_tile": (_I, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "pg_batch_autotune": (_I, [_P, C.c_char_p]),
+    "pg_batch_step_f32": (_I, [_P, C.POINTER(StepParams), _P, _P, _P, _P]),
     "pg_kernel_launches": (_I64, []),
     "pg_profile_enable": (_I, [_I]),
     "pg_profile_reset": (_I, []),

@@ -2,11 +2,11 @@
 //
 // One thread per output sample.  The back-traced position, clamps, floors
 // and the lerp form of math/interp.rs:7-36 are evaluated in the reference's
-// order with non-fusing round-to-nearest arithmetic, so a float (double)
-// result equals a sequential float (double) evaluation of the Rust code.
-// 3D is an extension: trilinear (math/interp.rs:23-36) with the per-axis
-// rules of the 2D code.
-#include "pg_internal.cuh"
+// order with non-fusing round-to-nearest arithmetic (pg_ops2d.cuh), so a
+// float (double) result equals a sequential float (double) evaluation of the
+// Rust code.  3D is an extension: trilinear (math/interp.rs:23-36) with the
+// per-axis rules of the 2D code.
+#include "pg_ops2d.cuh"
 
 namespace pg {
 
@@ -14,39 +14,6 @@ constexpr int kThreads = 256;
 
 #define GRID_STRIDE(i, n) for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (I)gridDim.x * blockDim.x)
 
-template <class T> __device__ __forceinline__ T bilerp(T a00, T a01, T a10, T a11, T s, T t) {
-    return lerp_ref(lerp_ref(a00, a01, s), lerp_ref(a10, a11, s), t);
-}
-
-// dec_fluid.rs:194-201 for one axis: p = clamp(pos - 0.5, 0, n - 1.00001);
-// i = floor(p); frac = p - i.  `hi` is n - 1.00001 rounded to T; when it
-// rounds to n-1 (float, n >= 257) the index is kept at n-2.
-template <class T, class I> __device__ __forceinline__ void cell_coord(T pos, I n, T hi, I& i0, T& frac) {
-    const T p = fmin(fmax(sub_rn(pos, T(0.5)), T(0)), hi);
-    I i = (I)floor(p);
-    if (i > n - 2) i = n - 2;
-    i0 = i;
-    frac = sub_rn(p, (T)i);
-}
-
-// dec_fluid.rs:236-244 / :274-281 for one axis of a face sample.
-template <class T, class I> __device__ __forceinline__ void face_coord(T pos, T off, I n, I& i0, I& i1, T& frac) {
-    const T q = sub_rn(pos, off);
-    const T p = fmax(floor(q), T(0));
-    const T last = (T)(n - 1);
-    i0 = (I)fmin(p, last);
-    i1 = (I)fmin(add_rn(p, T(1)), last);
-    // .min(1.0).max(0.0) with Rust's NaN rule: NaN.min(1) = 1.  Written out
-    // because the compiler turns fmax(fmin(v, 1), 0) into a saturate, which
-    // maps NaN to 0.
-    const T v = sub_rn(q, p);
-    frac = (v != v) ? T(1) : fmax(fmin(v, T(1)), T(0));
-}
-
-// pos + (-dt) * v  (integrate_euler, dec_fluid.rs:169-171)
-template <class T> __device__ __forceinline__ T back(T pos, T ndt, T v) { return add_rn(pos, mul_rn(ndt, v)); }
-
-// ---------------------------------------------------------------------------
 // advect, 2D (dec_fluid.rs:173-211)
 template <class T, class I>
 __global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, I h, I w,
@@ -55,16 +22,7 @@ __global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const 
     const T* vx = vel + (h + 1) * w;
     GRID_STRIDE(i, h * w) {
         const I y = i / w, x = i - y * w;
-        const T vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), T(2));
-        const T vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), T(2));
-        const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
-        const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
-        I ix, iy;
-        T u, v;
-        cell_coord(ppx, w, hix, ix, u);
-        cell_coord(ppy, h, hiy, iy, v);
-        const T* q0 = q + iy * w + ix;
-        dst[i] = bilerp(q0[0], q0[1], q0[w], q0[w + 1], u, v);
+        dst[i] = advect2d_at<T, I>(q, vy, vx, h, w, ndt, hix, hiy, y, x);
     }
 }
 
@@ -97,7 +55,6 @@ __global__ void k_advect_3d(T* __restrict__ dst, const T* __restrict__ q, const 
     }
 }
 
-// ---------------------------------------------------------------------------
 // advect_mac, 2D (dec_fluid.rs:213-291); src/dst/vel share the face layout.
 template <class T, class I>
 __global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, I h, I w,
@@ -106,37 +63,13 @@ __global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, 
     const T* vy = vel;
     const T* vx = vel + n0;
     GRID_STRIDE(i, nf) {
-        if (i >= n0) {  // x faces, qx dims (h, w+1): dec_fluid.rs:218-253
+        if (i >= n0) {  // x faces, qx dims (h, w+1)
             const I j = i - n0;
             const I y = j / wx, x = j - y * wx;
-            const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
-            const T velx = vx[y * wx + x];
-            const T vely = div_rn(add_rn(add_rn(add_rn(vy[y * w + xc], vy[(y + 1) * w + xc]), vy[y * w + xm]),
-                                         vy[(y + 1) * w + xm]),
-                                  T(4));
-            const T ppx = back(add_rn((T)x, T(0)), ndt, velx);
-            const T ppy = back(add_rn((T)y, T(0.5)), ndt, vely);
-            I x0, x1, y0, y1;
-            T s, t;
-            face_coord(ppx, T(0), w + 1, x0, x1, s);
-            face_coord(ppy, T(0.5), h, y0, y1, t);
-            const T* qx = src + n0;
-            dst[i] = bilerp(qx[y0 * wx + x0], qx[y0 * wx + x1], qx[y1 * wx + x0], qx[y1 * wx + x1], s, t);
-        } else {  // y faces, qy dims (h+1, w): dec_fluid.rs:255-290
+            dst[i] = advect_mac2d_x_at<T, I>(src + n0, vy, vx, h, w, ndt, y, x);
+        } else {  // y faces, qy dims (h+1, w)
             const I y = i / w, x = i - y * w;
-            const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
-            const T velx = div_rn(add_rn(add_rn(add_rn(vx[yc * wx + x], vx[yc * wx + x + 1]), vx[ym * wx + x]),
-                                         vx[ym * wx + x + 1]),
-                                  T(4));
-            const T vely = vy[y * w + x];
-            const T ppx = back(add_rn((T)x, T(0.5)), ndt, velx);
-            const T ppy = back(add_rn((T)y, T(0)), ndt, vely);
-            I x0, x1, y0, y1;
-            T s, t;
-            face_coord(ppx, T(0.5), w, x0, x1, s);
-            face_coord(ppy, T(0), h + 1, y0, y1, t);
-            const T* qy = src;
-            dst[i] = bilerp(qy[y0 * w + x0], qy[y0 * w + x1], qy[y1 * w + x0], qy[y1 * w + x1], s, t);
+            dst[i] = advect_mac2d_y_at<T, I>(src, vy, vx, h, w, ndt, y, x);
         }
     }
 }
@@ -157,16 +90,12 @@ __device__ __forceinline__ T sample_part(const T* __restrict__ q, I nz, I ny, I 
     return lerp_ref(b0, b1, u);
 }
 
-template <class T> __device__ __forceinline__ T avg4(T a, T b, T c, T d) {
-    return div_rn(add_rn(add_rn(add_rn(a, b), c), d), T(4));
-}
-
 // advect_mac, 3D extension
 template <class T, class I>
 __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, Dims D,
                                 T ndt) {
     const I d = (I)D.d, h = (I)D.h, w = (I)D.w;
-    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
+    const I nz = (I)D.nfz(), ny = (I)D.nfy();
     auto FX = [&](I z, I y, I x) { return nz + ny + (z * h + y) * (w + 1) + x; };
     auto FY = [&](I z, I y, I x) { return nz + (z * (h + 1) + y) * w + x; };
     auto FZ = [&](I z, I y, I x) { return (z * h + y) * w + x; };

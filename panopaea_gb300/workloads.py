@@ -87,6 +87,36 @@ WORKLOADS = {
 }
 
 
+def batch_grids(count=512, seed=3, sides=tuple(range(64, 513, 32)), max_circles=8, rmin=4, rmax=32, sigma=4.0):
+    """The batching configuration: `count` 2D grids, each side drawn
+    uniformly from `sides` (non-square allowed), 0..max_circles solid
+    circles of radius rmin..rmax cells, and a Gaussian smoke source (peak 1,
+    `sigma` cells) at a random cell adjacent to the domain boundary.
+    Returns (dims, cell_masks, sources) as lists of numpy arrays."""
+    rng = np.random.default_rng(seed)
+    dims, masks, sources = [], [], []
+    for _ in range(count):
+        h, w = int(rng.choice(sides)), int(rng.choice(sides))
+        y, x = np.mgrid[0:h, 0:w]
+        m = np.zeros((h, w), np.uint8)
+        for _ in range(int(rng.integers(0, max_circles + 1))):
+            r = rng.uniform(rmin, rmax)
+            cy, cx = rng.uniform(0, h), rng.uniform(0, w)
+            m |= (((y + 0.5 - cy) ** 2 + (x + 0.5 - cx) ** 2) < r * r).astype(np.uint8)
+        side = int(rng.integers(0, 4))  # bottom, top, left, right
+        if side < 2:
+            sy, sx = (0 if side == 0 else h - 1), int(rng.integers(0, w))
+        else:
+            sy, sx = int(rng.integers(0, h)), (0 if side == 2 else w - 1)
+        m[max(0, sy - 2):sy + 3, max(0, sx - 2):sx + 3] = 0  # keep the source cell fluid
+        src = np.exp(-((y - sy) ** 2 + (x - sx) ** 2) / (2 * sigma * sigma)).astype(np.float32)
+        src[m > 0] = 0.0
+        dims.append((h, w))
+        masks.append(m)
+        sources.append(src)
+    return dims, masks, sources
+
+
 def initial_state(name, dims=None):
     """(vel, density) host arrays for a named workload (dims overridable)."""
     spec = WORKLOADS[name]
