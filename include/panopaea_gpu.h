@@ -273,6 +273,29 @@ int pg_step_f64(const pg_grid* grid, const pg_step_params* params, double* vel, 
                 double* pressure, pg_pcg_stats* stats);
 
 /* ----------------------------------------------------------------------- */
+/* Sparse and diagonal matrix products (device pointers; stream may be NULL). */
+
+/* SparseMatrix::mul_vec (panopaea/src/sparse.rs:119-128): CSR with
+ * row_indices[rows + 1] and col_indices (int64, as the reference's usize);
+ * b[i] = left fold of acc + data[k] * x[col_indices[k]] over row i. */
+int pg_csr_mul_vec_f32(int64_t rows, const int64_t* row_indices, const int64_t* col_indices, const float* data,
+                       const float* x, float* b, void* cuda_stream);
+int pg_csr_mul_vec_f64(int64_t rows, const int64_t* row_indices, const int64_t* col_indices, const double* data,
+                       const double* x, double* b, void* cuda_stream);
+/* DiagonalMatrix::mul_vec (sparse.rs:20-25): b = x * a. */
+int pg_diag_mul_vec_f32(int64_t n, const float* a, const float* x, float* b, void* cuda_stream);
+int pg_diag_mul_vec_f64(int64_t n, const double* a, const double* x, double* b, void* cuda_stream);
+
+/* Headless image of a 2D cell field: imgproc::transfer (panopaea_utils/src/
+ * imgproc.rs:2-5) in f64 into three equal 8-bit channels, rows flipped as
+ * png::export writes them (png.rs:12), i.e. rgb[(y * w + x) * 3 + c] shows
+ * field[(h - 1 - y) * w + x]; the density dump of examples/dec_fluid.rs:143-164. */
+int pg_transfer_rgb8_f32(int64_t h, int64_t w, const float* field, double lower, double upper, uint8_t* rgb,
+                         void* cuda_stream);
+int pg_transfer_rgb8_f64(int64_t h, int64_t w, const double* field, double lower, double upper, uint8_t* rgb,
+                         void* cuda_stream);
+
+/* ----------------------------------------------------------------------- */
 /* Batches of independent 2D grids (extension; the reference steps a single
  * grid, examples/dec_fluid.rs:46-141).  Grids of different sizes are packed
  * back to back: grid i's cell field starts at cell_offsets[i] and its face

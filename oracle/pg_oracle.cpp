@@ -776,3 +776,44 @@ PGO_EXPORT long pgo_num_faces(int nd, long d, long h, long w) { return shape_of(
     }
 
 PGO_BOTH(PGO_DEFS)
+
+// ---------------------------------------------------------------------------
+// panopaea/src/sparse.rs:119-128 SparseMatrix::mul_vec (CSR, usize indices):
+// b[i] = fold(0, |acc, (k, j)| acc + data[start + k] * x[j]) over row i.
+template <class T> static void csr_mul_vec(long rows, const long* rowp, const long* cols, const T* data, const T* x, T* b) {
+    for (long i = 0; i < rows; ++i) {
+        T acc = T(0);
+        for (long k = rowp[i]; k < rowp[i + 1]; ++k) acc = acc + data[k] * x[cols[k]];
+        b[i] = acc;
+    }
+}
+
+// sparse.rs:20-25 DiagonalMatrix::mul_vec: b = x * a.
+template <class T> static void diag_mul_vec(long n, const T* a, const T* x, T* b) {
+    for (long i = 0; i < n; ++i) b[i] = x[i] * a[i];
+}
+
+// panopaea_utils/src/imgproc.rs:2-5 transfer, laid out as png.rs:6-18 writes
+// the image (row y of the image shows field row h-1-y), three channels.
+template <class T>
+static void transfer_rgb8(long h, long w, const T* f, double lo, double hi, unsigned char* rgb) {
+    for (long y = 0; y < h; ++y)
+        for (long x = 0; x < w; ++x) {
+            const double v = std::fmax(std::fmin((double)f[(h - 1 - y) * w + x], hi), lo);
+            const double s = (v - lo) / (hi - lo) * 255.0;
+            const unsigned char u = (s != s) ? 0 : (s <= 0.0 ? 0 : (s >= 255.0 ? 255 : (unsigned char)s));
+            for (int c = 0; c < 3; ++c) rgb[(y * w + x) * 3 + c] = u;
+        }
+}
+
+#define PGO_EXTRA(T, SFX)                                                                                       \
+    PGO_EXPORT void pgo_csr_mul_vec_##SFX(long rows, const long* rowp, const long* cols, const T* data,         \
+                                          const T* x, T* b) {                                                   \
+        csr_mul_vec(rows, rowp, cols, data, x, b);                                                              \
+    }                                                                                                           \
+    PGO_EXPORT void pgo_diag_mul_vec_##SFX(long n, const T* a, const T* x, T* b) { diag_mul_vec(n, a, x, b); }  \
+    PGO_EXPORT void pgo_transfer_rgb8_##SFX(long h, long w, const T* f, double lo, double hi, unsigned char* rgb) { \
+        transfer_rgb8(h, w, f, lo, hi, rgb);                                                                    \
+    }
+
+PGO_BOTH(PGO_EXTRA)

@@ -270,3 +270,28 @@ def cell_mask_to_faces(cell_solid):
 
 
 HAVE_LIB = os.path.exists(build_oracle.LIB)
+
+
+def csr_mul_vec(row_indices, col_indices, data, x):
+    """panopaea/src/sparse.rs:119-128 on the CPU."""
+    rows = len(row_indices) - 1
+    b = np.empty(rows, data.dtype)
+    rp = np.ascontiguousarray(row_indices, np.int64)
+    ci = np.ascontiguousarray(col_indices, np.int64)
+    getattr(lib(), "pgo_csr_mul_vec_" + _sfx(data))(C.c_long(rows), _p(rp), _p(ci), _p(_c(data)), _p(_c(x)), _p(b))
+    return b
+
+
+def diag_mul_vec(a, x):
+    b = np.empty_like(x)
+    getattr(lib(), "pgo_diag_mul_vec_" + _sfx(x))(C.c_long(x.size), _p(_c(a)), _p(_c(x)), _p(b))
+    return b
+
+
+def transfer_rgb8(field, lower, upper):
+    """imgproc.rs:2-5 + png.rs row flip: (h, w, 3) uint8 image rows."""
+    h, w = field.shape
+    out = np.empty((h, w, 3), np.uint8)
+    getattr(lib(), "pgo_transfer_rgb8_" + _sfx(field))(C.c_long(h), C.c_long(w), _p(_c(field)), C.c_double(lower),
+                                                       C.c_double(upper), _p(out))
+    return out

@@ -146,6 +146,9 @@ for _sfx in ("f32", "f64"):
         "pg_walls_" + _sfx: (_I, [_P, _P]),
         "pg_pcg_" + _sfx: (_I, [_P, _I, _P, _P, _I64, _D, _P, _P, _P, _D, C.POINTER(PcgStats)]),
         "pg_step_" + _sfx: (_I, [_P, C.POINTER(StepParams), _P, _P, _P, C.POINTER(PcgStats)]),
+        "pg_csr_mul_vec_" + _sfx: (_I, [_I64, _P, _P, _P, _P, _P, _P]),
+        "pg_diag_mul_vec_" + _sfx: (_I, [_I64, _P, _P, _P, _P]),
+        "pg_transfer_rgb8_" + _sfx: (_I, [_I64, _I64, _P, _D, _D, _P, _P]),
     })
 
 _lib = None
