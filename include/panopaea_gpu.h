@@ -111,7 +111,8 @@ typedef struct pg_step_params {
     double source_vy;             /* dec_fluid.rs:54 (20.0) */
     const void* source_field;     /* extension: device cell field, density = max(density, field); may be NULL */
     int32_t zero_solid_after_project; /* extension: re-zero solid faces after projection */
-    int32_t reserved;
+    int32_t advect_scheme;        /* density advection: 0 = the reference's (dec_fluid.rs:173-211);
+                                     extensions: 1 = MacCormack, 2 = BFECC (see pg_advect2_*) */
     pg_solver_params solver;      /* dec_fluid.rs:91-99: pcg(&(), .., 100, threshold, ..) */
 } pg_step_params;
 
@@ -199,6 +200,12 @@ int pg_divergence_rhs_f64(const pg_grid* grid, double* b, const double* vel);
  * bilinear (trilinear in 3D).  Needs every dimension >= 2. */
 int pg_advect_f32(const pg_grid* grid, float* dst, const float* src, double dt, const float* vel);
 int pg_advect_f64(const pg_grid* grid, double* dst, const double* src, double dt, const double* vel);
+/* Second-order advection of a cell scalar (extension): scheme 1 =
+ * MacCormack, scheme 2 = BFECC, both built from advect above and limited
+ * to the range of the source values of the first-order sample (falling
+ * back to it where they leave that range).  Scratch is library-owned. */
+int pg_advect2_f32(const pg_grid* grid, float* dst, const float* src, double dt, const float* vel, int scheme);
+int pg_advect2_f64(const pg_grid* grid, double* dst, const double* src, double dt, const double* vel, int scheme);
 /* advect_mac (examples/dec_fluid.rs:213-291): MAC face advection. */
 int pg_advect_mac_f32(const pg_grid* grid, float* dst, const float* src, double dt, const float* vel);
 int pg_advect_mac_f64(const pg_grid* grid, double* dst, const double* src, double dt, const double* vel);

@@ -588,7 +588,10 @@ struct pgo_step_params {
     int rel_stop;                // 0: abs threshold (pcg.rs:58-60); 1: threshold = rel_tol * ||b||inf
     double threshold, rel_tol;
     long max_iter;
+    int advect_scheme;           // density: 0 first order (reference), 1 MacCormack, 2 BFECC (extensions)
 };
+
+template <class T> static void advect2(T* dst, const T* q, T dt, const T* vel, int scheme, const Shape& s);
 
 struct pgo_step_stats {
     long iterations;
@@ -653,6 +656,7 @@ void step(const Shape& s, T* vel, T* density, T* pressure, const uint8_t* fs, co
         advect_3d(temp.data(), density, dt, vel, g);
         advect_mac_3d(vel_temp.data(), vel, dt, vel, g);
     }
+    if (prm.advect_scheme) advect2(temp.data(), density, dt, vel, prm.advect_scheme, s);
     std::memcpy(density, temp.data(), sizeof(T) * nc);
     std::memcpy(vel, vel_temp.data(), sizeof(T) * nf);
     if (prm.walls_after_advect) walls(vel, s);
@@ -776,6 +780,85 @@ PGO_EXPORT long pgo_num_faces(int nd, long d, long h, long w) { return shape_of(
     }
 
 PGO_BOTH(PGO_DEFS)
+
+// ---------------------------------------------------------------------------
+// Second-order limited advection of a cell scalar (extension; no reference
+// behaviour): MacCormack (scheme 1) and BFECC (scheme 2) built from the
+// first-order advect above; where the result leaves [min, max] of the
+// corner values the first-order sample of q interpolated, it falls back to
+// that sample.
+template <class T>
+static void corner_range(const T* q, const T* vel, T dt, const Shape& s, idx i, T* lo, T* hi) {
+    const T ndt = -dt;
+    if (s.nd == 2) {
+        const idx h = s.h, w = s.w;
+        const T* vy = vel;
+        const T* vx = vel + (h + 1) * w;
+        const idx y = i / w, x = i - y * w;
+        const T vcx = (vx[y * (w + 1) + x] + vx[y * (w + 1) + x + 1]) / T(2);
+        const T vcy = (vy[y * w + x] + vy[(y + 1) * w + x]) / T(2);
+        idx ix, iy;
+        T u, v;
+        cell_coord(((T)x + T(0.5)) + ndt * vcx, w, &ix, &u);
+        cell_coord(((T)y + T(0.5)) + ndt * vcy, h, &iy, &v);
+        const T* q0 = q + iy * w + ix;
+        *lo = std::fmin(std::fmin(q0[0], q0[1]), std::fmin(q0[w], q0[w + 1]));
+        *hi = std::fmax(std::fmax(q0[0], q0[1]), std::fmax(q0[w], q0[w + 1]));
+        return;
+    }
+    D3 g{s.d, s.h, s.w};
+    const idx w = g.w, hw = g.h * g.w;
+    const idx zy = i / w, x = i - zy * w, z = zy / g.h, y = zy - z * g.h;
+    const T vcx = (vel[g.fx(z, y, x)] + vel[g.fx(z, y, x + 1)]) / T(2);
+    const T vcy = (vel[g.fy(z, y, x)] + vel[g.fy(z, y + 1, x)]) / T(2);
+    const T vcz = (vel[g.fz(z, y, x)] + vel[g.fz(z + 1, y, x)]) / T(2);
+    idx ix, iy, iz;
+    T a, b, c;
+    cell_coord(((T)x + T(0.5)) + ndt * vcx, g.w, &ix, &a);
+    cell_coord(((T)y + T(0.5)) + ndt * vcy, g.h, &iy, &b);
+    cell_coord(((T)z + T(0.5)) + ndt * vcz, g.d, &iz, &c);
+    const T* q0 = q + iz * hw + iy * w + ix;
+    const T* q1 = q0 + hw;
+    *lo = std::fmin(std::fmin(std::fmin(q0[0], q0[1]), std::fmin(q0[w], q0[w + 1])),
+                    std::fmin(std::fmin(q1[0], q1[1]), std::fmin(q1[w], q1[w + 1])));
+    *hi = std::fmax(std::fmax(std::fmax(q0[0], q0[1]), std::fmax(q0[w], q0[w + 1])),
+                    std::fmax(std::fmax(q1[0], q1[1]), std::fmax(q1[w], q1[w + 1])));
+}
+
+template <class T> static void advect_any(T* dst, const T* src, T dt, const T* vel, const Shape& s) {
+    if (s.nd == 2) advect_2d(dst, src, dt, vel, s.h, s.w);
+    else advect_3d(dst, src, dt, vel, D3{s.d, s.h, s.w});
+}
+
+template <class T> static void advect2(T* dst, const T* q, T dt, const T* vel, int scheme, const Shape& s) {
+    const idx n = s.nc();
+    std::vector<T> q1(n), q2(n);
+    advect_any(q1.data(), q, dt, vel, s);
+    advect_any(q2.data(), q1.data(), -dt, vel, s);
+    if (scheme == 1) {
+        for (idx i = 0; i < n; ++i) {
+            T lo, hi;
+            corner_range(q, vel, dt, s, i, &lo, &hi);
+            const T v = q1[i] + T(0.5) * (q[i] - q2[i]);
+            dst[i] = (v < lo || v > hi || v != v) ? q1[i] : v;
+        }
+    } else {
+        for (idx i = 0; i < n; ++i) q2[i] = q[i] + T(0.5) * (q[i] - q2[i]);
+        advect_any(dst, q2.data(), dt, vel, s);
+        for (idx i = 0; i < n; ++i) {
+            T lo, hi;
+            corner_range(q, vel, dt, s, i, &lo, &hi);
+            if (dst[i] < lo || dst[i] > hi || dst[i] != dst[i]) dst[i] = q1[i];
+        }
+    }
+}
+
+#define PGO_ADV2(T, SFX)                                                                                       \
+    PGO_EXPORT void pgo_advect2_##SFX(T* dst, const T* src, double dt, const T* vel, int scheme, int nd, long d, \
+                                      long h, long w) {                                                        \
+        advect2(dst, src, (T)dt, vel, scheme, shape_of(nd, d, h, w));                                          \
+    }
+PGO_BOTH(PGO_ADV2)
 
 // ---------------------------------------------------------------------------
 // panopaea/src/sparse.rs:119-128 SparseMatrix::mul_vec (CSR, usize indices):

@@ -35,6 +35,7 @@ class StepParams(C.Structure):
         ("threshold", C.c_double),
         ("rel_tol", C.c_double),
         ("max_iter", C.c_long),
+        ("advect_scheme", C.c_int),
     ]
 
 
@@ -207,7 +208,7 @@ def step(vel, density, pressure, dims, params, face_solid=None):
 
 def step_params(dt=0.05, buoyancy=0.0, source=None, source_density=1.0, source_vy=20.0, source_field=None,
                 walls_after_advect=False, zero_solid_after_project=False, precond=0, rel_stop=False,
-                threshold=0.1, rel_tol=1e-6, max_iter=100):
+                threshold=0.1, rel_tol=1e-6, max_iter=100, advect_scheme=0):
     """StepParams; `source` = ((z0, y0, x0), (z1, y1, x1)) or None."""
     p = StepParams()
     p.dt = dt
@@ -227,7 +228,17 @@ def step_params(dt=0.05, buoyancy=0.0, source=None, source_density=1.0, source_v
     p.threshold = threshold
     p.rel_tol = rel_tol
     p.max_iter = max_iter
+    p.advect_scheme = advect_scheme
     return p
+
+
+def advect2(src, dt, vel, dims, scheme):
+    """Second-order limited advection of a cell scalar (1 MacCormack, 2 BFECC)."""
+    nd, d, h, w = _shape(dims)
+    out = np.empty_like(src)
+    getattr(lib(), "pgo_advect2_" + _sfx(src))(_p(out), _p(_c(src)), C.c_double(dt), _p(_c(vel)), int(scheme), nd,
+                                               C.c_long(d), C.c_long(h), C.c_long(w))
+    return out
 
 
 def reference_face_mask(dims, box=((70, 80), (50, 70))):

@@ -82,7 +82,7 @@ class StepParams(C.Structure):
         ("source_vy", C.c_double),
         ("source_field", C.c_void_p),
         ("zero_solid_after_project", C.c_int32),
-        ("reserved", C.c_int32),
+        ("advect_scheme", C.c_int32),
         ("solver", SolverParams),
     ]
 
@@ -142,6 +142,7 @@ for _sfx in ("f32", "f64"):
         "pg_divergence_rhs_" + _sfx: (_I, [_P, _P, _P]),
         "pg_advect_" + _sfx: (_I, [_P, _P, _P, _D, _P]),
         "pg_advect_mac_" + _sfx: (_I, [_P, _P, _P, _D, _P]),
+        "pg_advect2_" + _sfx: (_I, [_P, _P, _P, _D, _P, _I]),
         "pg_project_" + _sfx: (_I, [_P, _P, _P, _D, _I]),
         "pg_walls_" + _sfx: (_I, [_P, _P]),
         "pg_pcg_" + _sfx: (_I, [_P, _I, _P, _P, _I64, _D, _P, _P, _P, _D, C.POINTER(PcgStats)]),

@@ -184,6 +184,111 @@ template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src,
     return PG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Second-order advection of cell scalars (extension; the reference has only
+// the first-order scheme of examples/dec_fluid.rs:173-211).  With A(q, dt)
+// that scheme:
+//   MacCormack: q1 = A(q, dt), q2 = A(q1, -dt), q' = q1 + 0.5 (q - q2)
+//   BFECC:      q1 = A(q, dt), q2 = A(q1, -dt), qt = q + 0.5 (q - q2),
+//               q' = A(qt, dt)
+// both limited: where q' leaves [min, max] of the source values of q the
+// first-order sample interpolated from, q' = q1 (Selle et al. 2008).
+
+// min / max of the corner values of q at cell i's first-order back-trace.
+template <class T, class I>
+__device__ __forceinline__ void corner_range(const T* __restrict__ q, const T* __restrict__ vel, const Dims& D, T ndt,
+                                             T hix, T hiy, T hiz, I i, T& lo, T& hi) {
+    const I w = (I)D.w, h = (I)D.h;
+    if (D.nd == 2) {
+        const T* vy = vel;
+        const T* vx = vel + (h + 1) * w;
+        const I y = i / w, x = i - y * w;
+        const T vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), T(2));
+        const T vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), T(2));
+        I ix, iy;
+        T u, v;
+        cell_coord(back(add_rn((T)x, T(0.5)), ndt, vcx), w, hix, ix, u);
+        cell_coord(back(add_rn((T)y, T(0.5)), ndt, vcy), h, hiy, iy, v);
+        const T* q0 = q + iy * w + ix;
+        lo = fmin(fmin(q0[0], q0[1]), fmin(q0[w], q0[w + 1]));
+        hi = fmax(fmax(q0[0], q0[1]), fmax(q0[w], q0[w + 1]));
+        return;
+    }
+    const I d = (I)D.d, hw = h * w;
+    const I offy = (I)D.offy(), offx = (I)D.offx();
+    const I zy = i / w, x = i - zy * w;
+    const I z = zy / h, y = zy - z * h;
+    const T vcx = div_rn(add_rn(vel[offx + (z * h + y) * (w + 1) + x], vel[offx + (z * h + y) * (w + 1) + x + 1]), T(2));
+    const T vcy = div_rn(add_rn(vel[offy + (z * (h + 1) + y) * w + x], vel[offy + (z * (h + 1) + y + 1) * w + x]), T(2));
+    const T vcz = div_rn(add_rn(vel[(z * h + y) * w + x], vel[((z + 1) * h + y) * w + x]), T(2));
+    I ix, iy, iz;
+    T s, t, u;
+    cell_coord(back(add_rn((T)x, T(0.5)), ndt, vcx), w, hix, ix, s);
+    cell_coord(back(add_rn((T)y, T(0.5)), ndt, vcy), h, hiy, iy, t);
+    cell_coord(back(add_rn((T)z, T(0.5)), ndt, vcz), d, hiz, iz, u);
+    const T* q0 = q + iz * hw + iy * w + ix;
+    const T* q1 = q0 + hw;
+    lo = fmin(fmin(fmin(q0[0], q0[1]), fmin(q0[w], q0[w + 1])), fmin(fmin(q1[0], q1[1]), fmin(q1[w], q1[w + 1])));
+    hi = fmax(fmax(fmax(q0[0], q0[1]), fmax(q0[w], q0[w + 1])), fmax(fmax(q1[0], q1[1]), fmax(q1[w], q1[w + 1])));
+}
+
+// MacCormack: dst = q1 + 0.5 (q - q2), limited.
+template <class T, class I>
+__global__ void k_maccormack(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ q1,
+                             const T* __restrict__ q2, const T* __restrict__ vel, Dims D, T ndt, T hix, T hiy, T hiz) {
+    GRID_STRIDE(i, (I)D.nc()) {
+        T lo, hi;
+        corner_range<T, I>(q, vel, D, ndt, hix, hiy, hiz, i, lo, hi);
+        const T a = q1[i];
+        const T v = add_rn(a, mul_rn(T(0.5), sub_rn(q[i], q2[i])));
+        dst[i] = (v < lo || v > hi || v != v) ? a : v;
+    }
+}
+
+// BFECC: qt = q + 0.5 (q - q2)
+template <class T, class I> __global__ void k_bfecc_pre(T* qt, const T* q, const T* q2, I n) {  // qt may alias q2
+    GRID_STRIDE(i, n) qt[i] = add_rn(q[i], mul_rn(T(0.5), sub_rn(q[i], q2[i])));
+}
+
+// BFECC limiter: keep A(qt) where it stays in the first-order range, else q1.
+template <class T, class I>
+__global__ void k_bfecc_limit(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ q1,
+                              const T* __restrict__ vel, Dims D, T ndt, T hix, T hiy, T hiz) {
+    GRID_STRIDE(i, (I)D.nc()) {
+        T lo, hi;
+        corner_range<T, I>(q, vel, D, ndt, hix, hiy, hiz, i, lo, hi);
+        const T v = dst[i];
+        if (v < lo || v > hi || v != v) dst[i] = q1[i];
+    }
+}
+
+// dst = second-order advection of src; t1, t2 are caller scratch cell fields.
+template <class T>
+int launch_advect2(const pg_grid* g, T* dst, const T* src, double dt, const T* vel, int scheme, T* t1, T* t2) {
+    int rc;
+    if ((rc = launch_advect<T>(g, t1, src, dt, vel))) return rc;    // q1 = A(q, dt)
+    if ((rc = launch_advect<T>(g, t2, t1, -dt, vel))) return rc;    // q2 = A(q1, -dt)
+    const Dims& D = g->dims;
+    const T ndt = -(T)dt;
+    const T hix = (T)((double)D.w - 1.00001), hiy = (T)((double)D.h - 1.00001), hiz = (T)((double)D.d - 1.00001);
+    const int nb = grid_blocks(g, D.nc(), kThreads);
+    cudaStream_t s = g->stream;
+    if (D.nf() >= ((i64)1 << 31)) return bad_arg("second-order advection: grid too large for 32-bit indexing");
+    if (scheme == 1) {
+        PG_LAUNCH(KK_ADVECT, s, k_maccormack<T, int><<<nb, kThreads, 0, s>>>(dst, src, t1, t2, vel, D, ndt, hix, hiy, hiz));
+    } else {
+        PG_LAUNCH(KK_ADVECT, s, k_bfecc_pre<T, int><<<nb, kThreads, 0, s>>>(t2, src, t2, (int)D.nc()));
+        if ((rc = launch_advect<T>(g, dst, t2, dt, vel))) return rc;  // A(qt, dt)
+        PG_LAUNCH(KK_ADVECT, s, k_bfecc_limit<T, int><<<nb, kThreads, 0, s>>>(dst, src, t1, vel, D, ndt, hix, hiy, hiz));
+    }
+    PG_CHECK_LAUNCH();
+    return PG_OK;
+}
+
+template int launch_advect2<float>(const pg_grid*, float*, const float*, double, const float*, int, float*, float*);
+template int launch_advect2<double>(const pg_grid*, double*, const double*, double, const double*, int, double*,
+                                    double*);
+
 template int launch_advect<float>(const pg_grid*, float*, const float*, double, const float*);
 template int launch_advect<double>(const pg_grid*, double*, const double*, double, const double*);
 template int launch_advect_mac<float>(const pg_grid*, float*, const float*, double, const float*);

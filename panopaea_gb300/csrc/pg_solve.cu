@@ -20,6 +20,22 @@ template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* sr
 template <class T> int launch_buoyancy(const pg_grid* g, T* vel, const T* rho, double dt, double beta);
 template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, double dt, const T* vel);
 template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src, double dt, const T* vel);
+template <class T>
+int launch_advect2(const pg_grid* g, T* dst, const T* src, double dt, const T* vel, int scheme, T* t1, T* t2);
+
+// Second-order scalar advection with library-owned scratch.
+template <class T> static int advect2(pg_grid* g, T* dst, const T* src, double dt, const T* vel, int scheme) {
+    if (scheme != 1 && scheme != 2) return bad_arg("advect scheme must be 1 (MacCormack) or 2 (BFECC)");
+    const Dims& D = g->dims;
+    if (D.h < 2 || D.w < 2 || (D.nd == 3 && D.d < 2)) return bad_arg("pg_advect2: every dimension must be >= 2");
+    Extras* ex = extras_of(g);
+    void *t1, *t2;
+    int rc;
+    if ((rc = ex->buffer(Extras::kAdv1, sizeof(T) * (size_t)D.nc(), &t1)) ||
+        (rc = ex->buffer(Extras::kAdv2, sizeof(T) * (size_t)D.nc(), &t2)))
+        return rc;
+    return launch_advect2<T>(g, dst, src, dt, vel, scheme, (T*)t1, (T*)t2);
+}
 
 Extras* extras_of(pg_grid* g) {
     if (!g->extras) g->extras = new Extras();
@@ -480,7 +496,11 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure, pg_
     if (prm->source_enabled && (rc = launch_source_box<T>(g, rho, vel, prm))) return rc;
     if (prm->source_field && (rc = launch_source_field<T>(g, rho, (const T*)prm->source_field))) return rc;
     // advection with the old velocity (dec_fluid.rs:59-66)
-    if ((rc = launch_advect<T>(g, (T*)temp, rho, dt, vel))) return rc;
+    if (prm->advect_scheme == 0) {
+        if ((rc = launch_advect<T>(g, (T*)temp, rho, dt, vel))) return rc;
+    } else if ((rc = advect2<T>(g, (T*)temp, rho, dt, vel, prm->advect_scheme))) {
+        return rc;
+    }
     if ((rc = launch_advect_mac<T>(g, (T*)vtemp, vel, dt, vel))) return rc;
     PG_CUDA(cudaMemcpyAsync(rho, temp, sizeof(T) * nc, cudaMemcpyDeviceToDevice, g->stream));
     PG_CUDA(cudaMemcpyAsync(vel, vtemp, sizeof(T) * nf, cudaMemcpyDeviceToDevice, g->stream));
@@ -523,6 +543,15 @@ extern "C" int pg_solve_pressure_f32(const pg_grid* g, const pg_solver_params* p
     if (st) *st = s;
     return s.status;
 }
+
+#define PG_ADV2_ABI(T, SFX)                                                                                     \
+    extern "C" int pg_advect2_##SFX(const pg_grid* g, T* dst, const T* src, double dt, const T* vel, int scheme) { \
+        if (!g || !dst || !src || !vel) return bad_arg("pg_advect2: NULL argument");                           \
+        if (dst == src) return bad_arg("pg_advect2: dst must not alias src");                                  \
+        return advect2<T>(const_cast<pg_grid*>(g), dst, src, dt, vel, scheme);                                 \
+    }
+PG_ADV2_ABI(float, f32)
+PG_ADV2_ABI(double, f64)
 
 #define PG_STEP_ABI(T, SFX)                                                                                     \
     extern "C" int pg_step_##SFX(const pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure,     \

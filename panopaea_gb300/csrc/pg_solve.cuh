@@ -8,7 +8,7 @@ struct MgHierarchy;
 
 // Per-grid buffers of the solver and the step, grown on demand.
 struct Extras {
-    enum Slot { kR, kAp, kP0, kP1, kX64, kD, kRin, kTemp, kVelTemp, kB, kZ, kSlots };
+    enum Slot { kR, kAp, kP0, kP1, kX64, kD, kRin, kTemp, kVelTemp, kB, kZ, kAdv1, kAdv2, kSlots };
     void* buf_[kSlots] = {};
     size_t bytes_[kSlots] = {};
     void* small = nullptr;  // 256 B of device scalars

@@ -21,6 +21,16 @@ def advect(dst, src, timestep, vel):
     g._call("pg_advect_" + _sfx(dst.data), _ptr(dst.data), _ptr(src.data), C.c_double(timestep), _ptr(vel.data))
 
 
+MACCORMACK, BFECC = 1, 2
+
+
+def advect2(dst, src, timestep, vel, scheme=MACCORMACK):
+    """Second-order limited advection of a cell scalar (extension)."""
+    g = src.grid
+    g._call("pg_advect2_" + _sfx(dst.data), _ptr(dst.data), _ptr(src.data), C.c_double(timestep), _ptr(vel.data),
+            int(scheme))
+
+
 def advect_mac(dst, src, timestep, vel):
     """examples/dec_fluid.rs:213-291: MAC face advection."""
     g = src.grid
@@ -72,6 +82,7 @@ class StepConfig:
     source_field: object = None      # optional device cell field (Simplex2)
     walls_after_advect: bool = False
     zero_solid_after_project: bool = False
+    advect_scheme: int = 0           # 0 reference, 1 MacCormack, 2 BFECC (density)
     solver: SolverConfig = field(default_factory=SolverConfig)
 
     def to_c(self):
@@ -87,6 +98,7 @@ class StepConfig:
         p.source_vy = float(self.source_vy)
         p.source_field = self.source_field.data.data_ptr() if self.source_field is not None else None
         p.zero_solid_after_project = int(bool(self.zero_solid_after_project))
+        p.advect_scheme = int(self.advect_scheme)
         p.solver = self.solver.to_c()
         return p
 
