@@ -94,7 +94,10 @@ typedef struct pg_solver_params {
                               accumulation and projection run in double-float
                               (FP32 pairs, ~48-bit significand; GB300 runs
                               FP64 at 1/64 of the FP32 rate); 1 = native FP64 */
-    int32_t reserved;
+    int32_t initial_guess; /* extension, refine > 0 only: 1 = x holds an initial
+                              guess (e.g. pg_unet_guess_f32) and the first round
+                              solves for the correction of its FP64-class
+                              residual; 0 = start from x = 0 (pcg.rs:29) */
 } pg_solver_params;
 
 /* One fluid step, examples/dec_fluid.rs:46-141 (the PNG dump at :143-164
@@ -331,6 +334,60 @@ int pg_batch_autotune(pg_batch* batch, const char* cache_path);
  * first non-OK per-grid status. */
 int pg_batch_step_f32(pg_batch* batch, const pg_step_params* params, float* vel, float* density, float* pressure,
                       pg_pcg_stats* stats);
+
+/* ----------------------------------------------------------------------- */
+/* Learned pressure guess (extension, no reference counterpart: panopaea has
+ * no learned component).  A 3-level 3D conv U-Net, 16 base channels, BF16
+ * weights and activations with FP32 accumulation on the tensor cores, trained
+ * on the device by its own forward and backward kernels.  Inputs per cell:
+ * b / rms(b) and the open-face count / 6 of the grid's mask; output: a guess
+ * of the solution of A p = b (A = dt * the masked Laplacian), 0 on solid
+ * cells.  3D grids only; every side a multiple of 4 and >= 16. */
+
+typedef struct pg_unet pg_unet;
+
+typedef struct pg_adam_params {
+    double lr;
+    double beta1;
+    double beta2;
+    double eps;
+    double grad_scale;     /* gradients are multiplied by this (1 / samples) */
+} pg_adam_params;
+
+/* Number of FP32 parameters: 10 conv weights [27][c_in][c_out] in layer
+ * order, then the 16 weights of the 1x1 output layer. */
+int64_t pg_unet_num_params(void);
+/* Network and activations for grids of shape (d, h, w). */
+int pg_unet_create(int64_t d, int64_t h, int64_t w, pg_unet** out);
+int pg_unet_destroy(pg_unet* net);
+int pg_unet_set_stream(pg_unet* net, void* cuda_stream);
+/* Host parameters (pg_unet_num_params floats) and the output scale (the
+ * typical |p| * dt / rms(b) of the training data); resets the Adam state. */
+int pg_unet_set_params(pg_unet* net, const float* host_params, double out_scale);
+int pg_unet_get_params(const pg_unet* net, float* host_params, double* out_scale);
+/* Accumulated gradients (host copy) and their reset. */
+int pg_unet_get_grads(const pg_unet* net, float* host_grads);
+int pg_unet_zero_grads(pg_unet* net);
+/* Training loss: 0 = mean squared error of the normalised guess q on open
+ * cells, sum e^2 / cells; 1 (default) = its energy norm, sum e (A1 e) / cells
+ * with A1 the masked Laplacian at dt = 1 (the error norm CG reduces, blind
+ * to the constant null-space offset); e = q - p_true dt / (rms(b) out_scale). */
+int pg_unet_set_loss(pg_unet* net, int kind);
+/* Forward pass and loss for one sample (device b, device target p_true,
+ * the grid's solid mask); adds the gradient of the loss to the accumulated
+ * gradients.  loss may be NULL (else synchronises). */
+int pg_unet_accumulate_f32(pg_unet* net, const pg_grid* grid, const float* b, const float* p_true, double dt,
+                           double* loss);
+/* One Adam step on the accumulated gradients, then zeroes them. */
+int pg_unet_adam_step(pg_unet* net, const pg_adam_params* params);
+/* p = the network's raw output for b (no step-length scaling).  Asynchronous. */
+int pg_unet_forward_f32(pg_unet* net, const pg_grid* grid, const float* b, double dt, float* p);
+/* Guess for A x = b: x = alpha d with d = the network's output for b and
+ * alpha = (d.b) / (d.Ad), the step that minimises the energy norm of the
+ * error along d (so the guess is never worse than x = 0 in that norm);
+ * corrections > 0 repeats it on the residual (x += alpha d, d = net(b - Ax)).
+ * Asynchronous. */
+int pg_unet_guess_f32(pg_unet* net, const pg_grid* grid, const float* b, double dt, int corrections, float* x);
 
 /* ----------------------------------------------------------------------- */
 /* Instrumentation (no reference counterpart; the reference only prints

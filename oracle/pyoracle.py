@@ -306,3 +306,42 @@ def transfer_rgb8(field, lower, upper):
     getattr(lib(), "pgo_transfer_rgb8_" + _sfx(field))(C.c_long(h), C.c_long(w), _p(_c(field)), C.c_double(lower),
                                                        C.c_double(upper), _p(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# The learned pressure-guess network (oracle/unet_oracle.cpp).
+
+def unet_num_params():
+    lib().pgo_unet_num_params.restype = C.c_long
+    return int(lib().pgo_unet_num_params())
+
+
+def unet_run(params, out_scale, dt, dims, b, face_solid=None, p_true=None, want_grad=False, loss_kind=1):
+    """Forward pass (guess p), and with `p_true` the loss (0 MSE, 1 energy
+    norm) and, if asked, the gradient of every parameter.  float32 arrays run
+    the bf16-storage mode of the GPU kernels, float64 arrays the exact mode.
+    Returns (p, loss, grad)."""
+    d, h, w = dims
+    dt_ = np.float32 if params.dtype == np.float32 else np.float64
+    params = np.ascontiguousarray(params, dt_)
+    b = np.ascontiguousarray(b, dt_)
+    if face_solid is not None:
+        face_solid = np.ascontiguousarray(face_solid, np.uint8)
+    nopen = open_face_count(dims, face_solid, np.float64).astype(np.uint8)
+    p = np.empty(dims, dt_)
+    grad = np.empty(params.size, dt_) if (want_grad and p_true is not None) else None
+    loss = C.c_double(0.0)
+    if p_true is not None:
+        p_true = np.ascontiguousarray(p_true, dt_)
+    fn = getattr(lib(), "pgo_unet_run_" + _sfx(params))
+    fn.restype = None
+    fn(_p(params), C.c_double(out_scale), C.c_double(dt), C.c_long(d), C.c_long(h), C.c_long(w), _p(b), _p(nopen),
+       _p(face_solid), int(loss_kind), _p(p_true), _p(p), _p(grad), C.byref(loss))
+    return p, (loss.value if p_true is not None else None), grad
+
+
+def bf16_round(x):
+    fn = lib().pgo_bf16_round
+    fn.restype = C.c_float
+    fn.argtypes = [C.c_float]
+    return np.array([fn(float(v)) for v in np.ravel(x)], np.float32).reshape(np.shape(x))

@@ -66,7 +66,7 @@ class SolverParams(C.Structure):
         ("mg_levels", C.c_int32),
         ("mg_smooth", C.c_int32),
         ("fp64_native", C.c_int32),
-        ("reserved", C.c_int32),
+        ("initial_guess", C.c_int32),
     ]
 
 
@@ -85,6 +85,11 @@ class StepParams(C.Structure):
         ("advect_scheme", C.c_int32),
         ("solver", SolverParams),
     ]
+
+
+class AdamParams(C.Structure):
+    _fields_ = [("lr", C.c_double), ("beta1", C.c_double), ("beta2", C.c_double), ("eps", C.c_double),
+                ("grad_scale", C.c_double)]
 
 
 _P = C.c_void_p
@@ -123,6 +128,19 @@ _SIGS = {
     "pg_batch_set_tile": (_I, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "pg_batch_autotune": (_I, [_P, C.c_char_p]),
     "pg_batch_step_f32": (_I, [_P, C.POINTER(StepParams), _P, _P, _P, _P]),
+    "pg_unet_num_params": (_I64, []),
+    "pg_unet_create": (_I, [_I64, _I64, _I64, C.POINTER(_P)]),
+    "pg_unet_destroy": (_I, [_P]),
+    "pg_unet_set_stream": (_I, [_P, _P]),
+    "pg_unet_set_params": (_I, [_P, _P, _D]),
+    "pg_unet_get_params": (_I, [_P, _P, C.POINTER(_D)]),
+    "pg_unet_get_grads": (_I, [_P, _P]),
+    "pg_unet_zero_grads": (_I, [_P]),
+    "pg_unet_accumulate_f32": (_I, [_P, _P, _P, _P, _D, C.POINTER(_D)]),
+    "pg_unet_adam_step": (_I, [_P, C.POINTER(AdamParams)]),
+    "pg_unet_guess_f32": (_I, [_P, _P, _P, _D, _I, _P]),
+    "pg_unet_forward_f32": (_I, [_P, _P, _P, _D, _P]),
+    "pg_unet_set_loss": (_I, [_P, _I]),
     "pg_kernel_launches": (_I64, []),
     "pg_profile_enable": (_I, [_I]),
     "pg_profile_reset": (_I, []),

@@ -398,20 +398,48 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     out.status = PG_NOT_CONVERGED;
     i64 iters = 0;
     int rounds = 0;
-    while (rounds < prm->refine) {
-        // Round 0 solves A d = b itself (x = 0, so the residual is b exactly
-        // and no residual kernel is needed); later rounds solve for the
-        // correction of the FP64-class residual r = b - A x.
-        CgBuffers<float> buf{(float*)d, rounds == 0 ? b : (const float*)rin, (float*)rr, (float*)ap,
+    const bool guess = prm->initial_guess != 0;
+    bool done = false;
+    if (guess) {
+        // ||b||inf from the residual of x = 0, then the residual of the guess.
+        if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &bmax))) return rc;
+        target = prm->rel_stop ? prm->rel_tol * bmax : prm->threshold;
+        rmax = bmax;
+        if (bmax == 0.0 || !std::isfinite(bmax)) {
+            out.status = bmax == 0.0 ? PG_OK : PG_NAN_DETECTED;
+            done = true;
+        } else {
+            if (native)
+                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, x, n));
+            else
+                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_add<<<nb, kThreads, 0, g->stream>>>(xh, xl, x, n));
+            PG_CHECK_LAUNCH();
+            if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
+            if (!std::isfinite(rmax)) {
+                out.status = PG_NAN_DETECTED;
+                done = true;
+            } else if (rmax <= target) {
+                out.status = PG_OK;
+                done = true;
+            }
+        }
+    }
+    while (!done && rounds < prm->refine) {
+        // Round 0 without a guess solves A d = b itself (x = 0, so the
+        // residual is b exactly and no residual kernel is needed); other
+        // rounds solve for the correction of the FP64-class residual
+        // r = b - A x.
+        const bool from_b = rounds == 0 && !guess;
+        CgBuffers<float> buf{(float*)d, from_b ? b : (const float*)rin, (float*)rr, (float*)ap,
                              {(float*)p0, (float*)p1}};
         CgConfig cfg{prm->precond, prm->max_iter, 0.0, 0.0, dt, prm->check_every, 1};
-        if (rounds == 0 && !prm->rel_stop) {
+        if (from_b && !prm->rel_stop) {
             cfg.threshold = 0.5 * prm->threshold;
         } else {
             // Reach half the outer target, but never ask FP32 CG for more
             // than ~1e-5 relative per round.
             double inner = prm->inner_rel_tol > 0 ? prm->inner_rel_tol
-                           : rounds == 0      ? 0.5 * prm->rel_tol
+                           : from_b           ? 0.5 * prm->rel_tol
                                               : 0.5 * target / rmax;
             cfg.rel_tol = std::min(std::max(inner, 1e-5), 0.5);
         }
@@ -423,7 +451,7 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
         if (rc) return rc;
         iters += s.iterations;
         ++rounds;
-        if (rounds == 1) {
+        if (rounds == 1 && !guess) {
             bmax = s.b_max;
             target = prm->rel_stop ? prm->rel_tol * bmax : prm->threshold;
             rmax = bmax;
@@ -472,6 +500,7 @@ template <class T>
 int solve_pressure(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, double dt, pg_pcg_stats* st) {
     if (prm->precond < PG_PRECOND_NONE || prm->precond > PG_PRECOND_MG) return bad_arg("solver: unknown precond");
     if (prm->max_iter < 0) return bad_arg("solver: max_iter < 0");
+    if (prm->initial_guess && prm->refine <= 0) return bad_arg("solver: initial_guess needs refine > 0");
     if (prm->refine > 0) {
         if (sizeof(T) != 4) return bad_arg("solver: refinement is for f32 fields");
         return solve_refined(g, prm, (float*)x, (const float*)b, dt, st);

@@ -51,6 +51,7 @@ class SolverConfig:
     mg_levels: int = 0
     mg_smooth: int = 0
     fp64_native: bool = False
+    initial_guess: bool = False      # refine > 0: x holds a starting guess
 
     def to_c(self):
         p = N.SolverParams()
@@ -65,6 +66,7 @@ class SolverConfig:
         p.mg_levels = int(self.mg_levels)
         p.mg_smooth = int(self.mg_smooth)
         p.fp64_native = int(bool(self.fp64_native))
+        p.initial_guess = int(bool(self.initial_guess))
         return p
 
 
