@@ -73,6 +73,10 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-PCG comparison (profiling runs)")
     ap.add_argument("--cpu-cap", type=int, default=16, help="CG iterations per CPU sample")
+    ap.add_argument("--pairs", type=int, default=1000, help="learned_3d_128: training pairs (streamed)")
+    ap.add_argument("--held", type=int, default=32, help="learned_3d_128: held-out grids")
+    ap.add_argument("--gen", default="mg", choices=["mg", "plain"], help="learned_3d_128: solver of the pairs")
+    ap.add_argument("--batch-count", type=int, default=512, help="batch_512: number of grids")
     return ap.parse_args()
 
 
@@ -201,15 +205,22 @@ def ncu_traffic(kind, workload):
     return None
 
 
-def solver_cfgs(pg, rel_tol, have_mg):
+def solver_cfgs(pg, spec, have_mg):
+    """(chosen, comparison): MG-PCG in FP64 refinement, and the plain FP32
+    PCG of the reference (or Jacobi-PCG in refinement, where the workload
+    names that comparison)."""
+    rel_tol = spec["rel_tol"]
     chosen = pg.SolverConfig(precond=2 if have_mg else 1, rel_stop=True, rel_tol=rel_tol, max_iter=20000, refine=4)
-    plain = pg.SolverConfig(precond=0, rel_stop=True, rel_tol=rel_tol, max_iter=200000)
-    return chosen, plain
+    if spec.get("compare") == "jacobi":
+        other = pg.SolverConfig(precond=1, rel_stop=True, rel_tol=rel_tol, max_iter=200000, refine=4)
+    else:
+        other = pg.SolverConfig(precond=0, rel_stop=True, rel_tol=rel_tol, max_iter=200000)
+    return chosen, other
 
 
-def step_cfg(pg, spec, solver):
+def step_cfg(pg, spec, solver, source_field=None):
     return pg.StepConfig(dt=spec["dt"], buoyancy=spec["buoyancy"], source_enabled=False, walls_after_advect=True,
-                         zero_solid_after_project=True, solver=solver)
+                         zero_solid_after_project=True, source_field=source_field, solver=solver)
 
 
 def have_mg(pg, grid):
@@ -328,9 +339,16 @@ def ours(args, spec, dims):
     cells = int(np.prod(dims))
     vel0, rho0 = W.initial_state(args.workload, dims)
     grid = pg.Grid3d(dims) if len(dims) == 3 else pg.Grid2d(dims)
+    src = None
+    if args.workload.startswith("sphere_3d"):
+        mask, src_h = W.sphere_plume(dims, spec["sphere_r"], spec["disk_r"])
+        grid.set_solid_cells(mask)
+        src = pg.Simplex2(grid, torch.from_numpy(src_h).cuda())
+        del mask, src_h
     mg = have_mg(pg, grid)
-    chosen, plain = solver_cfgs(pg, spec["rel_tol"], mg)
-    cfg_c, cfg_p = step_cfg(pg, spec, chosen), step_cfg(pg, spec, plain)
+    chosen, plain = solver_cfgs(pg, spec, mg)
+    cfg_c, cfg_p = step_cfg(pg, spec, chosen, src), step_cfg(pg, spec, plain, src)
+    compare_key = "jacobi_pcg" if spec.get("compare") == "jacobi" else "plain_fp32_pcg"
 
     def fresh():
         return (pg.Simplex1(grid, torch.from_numpy(vel0).cuda()), pg.Simplex2(grid, torch.from_numpy(rho0).cuda()),
@@ -423,7 +441,7 @@ def ours(args, spec, dims):
                 "dominant_overall": max(kinds, key=lambda k: kinds[k][0])}
     # --- CPU baseline (rank 0, N = 1) ---------------------------------------
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu and spec.get("cpu"):
         from oracle import pyoracle as O
 
         s = cpu_sample(O, dims, spec, vel0, rho0, args.cpu_cap)
@@ -444,7 +462,7 @@ def ours(args, spec, dims):
                        "l2": "inputs larger than L2 (%.0f MB of fields per step)" % ((vel0.size + rho0.size * 3) * 4 / 1e6)},
             "iterations_per_step": its,
             "true_residual_rel": [s["true_residual_max"] / s["b_max"] if s["b_max"] else 0.0 for s in stats],
-            "plain_fp32_pcg": plain_out,
+            compare_key: plain_out,
             "roofline": roof,
             "profiled_ms_per_step": ms_prof / args.steps,
             "kernels_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in sorted(kinds.items(), key=lambda kv: -kv[1][0])},
@@ -454,10 +472,250 @@ def ours(args, spec, dims):
     dist.close()
 
 
+# ---------------------------------------------------------------------------
+# Learned initial guess (128^3 grids with solid boxes)
+
+def unet_forward_flops(dims):
+    """Multiply-adds x 2 of the network's convolutions for one forward pass
+    on grids of `dims` (layer 0 counted with its 2 real input channels)."""
+    from panopaea_gb300 import learned
+
+    v = [int(np.prod([n >> lvl for n in dims])) for lvl in range(3)]
+    level = (0, 0, 1, 1, 2, 2, 1, 1, 0, 0)
+    fl = 0
+    for k in range(10):
+        cin = 2 if k == 0 else learned.CIN[k]
+        fl += 2 * 27 * cin * learned.COUT[k] * v[level[k]]
+    return fl + 2 * 16 * v[0]
+
+
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def bench_learned(args):
+    """128^3 grids, 1-6 solid boxes, filtered-noise divergence.  The network
+    is trained on --pairs freshly generated (b, p) pairs (streamed), then
+    --held held-out grids are solved to relative 1e-6 by plain CG and by
+    MG-PCG (both in FP64 refinement), each from x = 0 and from the learned
+    guess.  A step = one pressure solve; value = the learned-guess + plain
+    CG form; every form is reported."""
+    import ctypes as C
+
+    import torch
+
+    import panopaea_gb300 as pg
+    from panopaea_gb300 import learned
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = Dist(ws, rank, local, "nccl")
+    lib = pg.load()
+    dims = tuple(int(v) for v in args.dims.split(",")) if args.dims else (128, 128, 128)
+    cells = int(np.prod(dims))
+    g = pg.Grid3d(dims)
+    dt = 1.0
+    gen_solver = pg.SolverConfig(precond=2 if args.gen == "mg" else 0, rel_stop=True, rel_tol=1e-6,
+                                 max_iter=100000, refine=8)
+    first = [learned.training_pair(g, 1_000_000 + i, dt, gen_solver)[:2] for i in range(16)]
+    scale = learned.estimate_out_scale(first, dt)
+    del first
+    net = learned.PressureNet(dims, out_scale=scale, seed=1)
+    losses, t_gen, t_train = learned.train_streaming(net, g, range(2_000_000 + 10_000 * rank,
+                                                                   2_000_000 + 10_000 * rank + args.pairs),
+                                                     dt, gen_solver, batch=8, lr=1e-3)
+    forms = {
+        "plain_cg": (pg.SolverConfig(precond=0, rel_stop=True, rel_tol=1e-6, max_iter=100000, refine=8), None),
+        "learned_guess_plain_cg": (pg.SolverConfig(precond=0, rel_stop=True, rel_tol=1e-6, max_iter=100000,
+                                                   refine=8), 1),
+        "mg_pcg": (pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4), None),
+        "learned_guess_mg_pcg": (pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000,
+                                                 refine=4), 0),
+    }
+    res = {k: {"ms": [], "iterations": [], "true_residual_rel": []} for k in forms}
+    held = [learned.training_pair(g, 9_000_000 + i, dt, solve=False)[::2] for i in range(args.held)]
+    stream = torch.cuda.current_stream()
+    x = g.new_simplex_2()
+    # warm-up (graphs, workspaces)
+    g.set_solid_cells(held[0][1])
+    for name, (solver, corr) in forms.items():
+        for _ in range(2):
+            (pg.solve_pressure(g, x, held[0][0], dt, solver) if corr is None
+             else learned.solve_with_guess(net, g, x, held[0][0], dt, solver, corr))
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = lib.pg_kernel_launches()
+    dist.barrier()
+    for b, mask in held:
+        g.set_solid_cells(mask)
+        for name, (solver, corr) in forms.items():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            st = (pg.solve_pressure(g, x, b, dt, solver) if corr is None
+                  else learned.solve_with_guess(net, g, x, b, dt, solver, corr))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            res[name]["ms"].append(e0.elapsed_time(e1))
+            res[name]["iterations"].append(st["iterations"])
+            res[name]["true_residual_rel"].append(st["true_residual_max"] / st["b_max"] if st["b_max"] else 0.0)
+    dist.barrier()
+    launches = lib.pg_kernel_launches() - launches0
+    clk = clocks.stop()
+    out_forms = {}
+    for name, r in res.items():
+        ms = dist.max(float(np.mean(r["ms"])))
+        out_forms[name] = {"value": ws * cells / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_solve": ms,
+                           "mean_iterations": float(np.mean(r["iterations"])),
+                           "max_true_residual_rel": float(np.max(r["true_residual_rel"]))}
+    # e2e: b from pinned host memory, guess + plain CG, x back to the host
+    hb = held[0][0].data.cpu().pin_memory()
+    hx = torch.empty_like(hb).pin_memory()
+    g.set_solid_cells(held[0][1])
+    b = g.new_simplex_2()
+    solver, corr = forms["learned_guess_plain_cg"]
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ne = min(4, args.held)
+    e0.record(stream)
+    for _ in range(ne):
+        b.data.copy_(hb, non_blocking=True)
+        learned.solve_with_guess(net, g, x, b, dt, solver, corr)
+        hx.copy_(x.data, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e = dist.max(e0.elapsed_time(e1) / ne)
+    # roofline: the network's convolutions in one guess (tensor-core bound)
+    lib.pg_profile_reset()
+    lib.pg_profile_enable(1)
+    net.guess(g, b, dt, x, 0)
+    torch.cuda.synchronize()
+    lib.pg_profile_enable(0)
+    kinds = {}
+    for k in range(lib.pg_profile_num_kinds()):
+        t, n = C.c_double(), C.c_int64()
+        lib.pg_profile_read(k, C.byref(t), C.byref(n))
+        if n.value:
+            kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
+    peak, src = bf16_peak()
+    conv_ms, conv_n = kinds.get("unet_conv", (float("nan"), 0))
+    flops = unet_forward_flops(dims)
+    achieved = flops / (conv_ms / 1e3) / 1e12
+    if rank == 0:
+        v = out_forms["learned_guess_plain_cg"]["value"]
+        out = {
+            "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.held, "warmup": 2,
+            "ms_per_step": out_forms["learned_guess_plain_cg"]["ms_per_solve"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 fields, bf16 network", "data": "synthetic",
+            "config": {"workload": "learned_3d_128", "dims": list(dims), "cells": cells, "rel_tol": 1e-6,
+                       "step": "one pressure solve", "train_pairs": args.pairs, "held_out_grids": args.held,
+                       "pair_solver": "MG-PCG in FP64 refinement to 1e-6" if args.gen == "mg"
+                       else "plain CG in FP64 refinement to 1e-6",
+                       "form": "learned guess + 1 learned correction, then plain CG in FP64 refinement",
+                       "parallelism": "replicas x%d" % ws, "l2": "fields of 8 MB per grid: L2-resident"},
+            "forms": out_forms,
+            "speedup_vs_plain_cg": out_forms["plain_cg"]["ms_per_solve"] / out_forms["learned_guess_plain_cg"]["ms_per_solve"],
+            "iterations_saved_vs_plain_cg": 1.0 - out_forms["learned_guess_plain_cg"]["mean_iterations"] /
+            out_forms["plain_cg"]["mean_iterations"],
+            "training": {"pairs": args.pairs, "loss_first_100": float(np.mean(losses[:100])),
+                         "loss_last_100": float(np.mean(losses[-100:])), "seconds_generating": t_gen,
+                         "seconds_training": t_train, "ms_per_training_sample": 1e3 * t_train / max(1, args.pairs),
+                         "loss": "energy norm"},
+            "roofline": {"bound": "tensor", "kernel": "unet_conv", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": src, "traffic": None,
+                         "algorithmic_flops_per_guess": flops, "conv_ms_per_guess": conv_ms, "launches": conv_n},
+            "kernels_ms_one_guess": {k: {"ms": t, "launches": n} for k, (t, n) in kinds.items()},
+            "cpu_baseline": None,
+            "e2e": {"value": ws * cells / (ms_e / 1e3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": 4 * cells,
+                    "d2h_bytes_per_step": 4 * cells, "ms_per_step": ms_e},
+            "clocks": clk, "gpu_launches": int(launches),
+        }
+        print(json.dumps(out), flush=True)
+    dist.close()
+
+
+# ---------------------------------------------------------------------------
+# Batching: 512 independent 2D grids
+
+def bench_batch(args):
+    """512 2D grids, sides from {64, 96, ..., 512}, 0-8 solid circles, a
+    Gaussian source at a boundary-adjacent cell, dt 0.5, buoyancy 1; every
+    stage one launch over all grids (the batch path), Jacobi-PCG to relative
+    1e-6 per grid; tile shape from the autotuner.  Grids are partitioned by
+    cost across ranks (no data exchange)."""
+    import torch
+
+    import panopaea_gb300 as pg
+    from panopaea_gb300 import workloads as W
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = Dist(ws, rank, local, "nccl")
+    lib = pg.load()
+    dims_all, masks_all, srcs_all = W.batch_grids(args.batch_count)
+    part = pg.partition_by_cost(dims_all, ws)[rank]
+    dims = [dims_all[i] for i in part]
+    B = pg.Batch2d(dims)
+    B.set_solid_cells([masks_all[i] for i in part])
+    t0 = time.time()
+    tile = B.autotune()
+    t_tune = time.time() - t0
+    v, rho, p = B.new_faces(), B.new_cells(), B.new_cells()
+    src = torch.from_numpy(B.pack_cells([srcs_all[i] for i in part])).cuda()
+    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True,
+                        solver=pg.SolverConfig(precond=1, rel_stop=True, rel_tol=1e-6, max_iter=100000))
+    for _ in range(args.warmup):
+        B.step(cfg, v, rho, p, source_field=src)
+    stream = torch.cuda.current_stream()
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = lib.pg_kernel_launches()
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = [B.step(cfg, v, rho, p, source_field=src) for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    launches = lib.pg_kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = dist.max(e0.elapsed_time(e1))
+    total_cells = sum(h * w for h, w in dims_all)
+    value = total_cells * args.steps / (ms / 1e3) / 1e6
+    its = [max(s["iterations"] for s in st) for st in stats]
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch_512", "grids": len(dims_all), "cells": total_cells, "dt": 0.5,
+                       "rel_tol": 1e-6, "form": "batched Jacobi-PCG, one launch per stage over all grids, "
+                                                "device-side graph loop",
+                       "tile": list(tile), "autotune_s": t_tune, "parallelism": "cost-partitioned x%d" % ws,
+                       "l2": "fields of %.0f MB per step" % (total_cells * 4 * 6 / 1e6)},
+            "max_iterations_per_step": its,
+            "statuses": sorted(set(s["status"] for st in stats for s in st)),
+            "cpu_baseline": None, "roofline": None, "e2e": None, "clocks": clk, "gpu_launches": int(launches),
+        }
+        print(json.dumps(out), flush=True)
+    dist.close()
+
+
 def main():
     args = parse_args()
     from panopaea_gb300 import workloads as W
 
+    if args.impl != "reference" and args.workload == "learned_3d_128":
+        return bench_learned(args)
+    if args.impl != "reference" and args.workload == "batch_512":
+        return bench_batch(args)
     spec = W.WORKLOADS[args.workload]
     dims = tuple(int(v) for v in args.dims.split(",")) if args.dims else tuple(spec["dims"])
     if args.impl == "reference":

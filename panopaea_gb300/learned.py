@@ -200,10 +200,11 @@ def noise_velocity(dims, seed, umax=2.0, passes=3):
     return torch.cat([p.reshape(-1) for p in parts]) * (umax / m)
 
 
-def training_pair(grid, seed, dt=1.0, solver=None, umax=2.0):
+def training_pair(grid, seed, dt=1.0, solver=None, umax=2.0, solve=True):
     """Set the grid's mask to a seeded box configuration and return
     (b, p, mask, stats): b = -div u of a seeded filtered-noise velocity, p
-    its pressure to relative 1e-6 (by default plain CG in FP64 refinement)."""
+    its pressure to relative 1e-6 (by default plain CG in FP64 refinement;
+    p and stats are None with solve=False)."""
     rng = np.random.default_rng(seed)
     dims = grid.dim()
     mask = box_obstacles(dims, rng)
@@ -211,6 +212,9 @@ def training_pair(grid, seed, dt=1.0, solver=None, umax=2.0):
     vel = Simplex1(grid, noise_velocity(dims, int(rng.integers(1 << 62)), umax))
     b = grid.new_simplex_2()
     grid.divergence_rhs(b, vel)
+    del vel
+    if not solve:
+        return b, None, mask, None
     p = grid.new_simplex_2()
     solver = solver or SolverConfig(rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=8)
     st = solve_pressure(grid, p, b, dt, solver)
@@ -252,5 +256,36 @@ def train(net, grid, pairs, dt, epochs=1, batch=4, lr=1e-3, lr_end=None, log=Non
     return hist
 
 
+def train_streaming(net, grid, seeds, dt, solver=None, batch=8, lr=1e-3, lr_end=None, log=None):
+    """One pass over freshly generated pairs (generated, trained on, then
+    dropped: nothing is stored), `batch` samples per Adam step, cosine
+    learning-rate decay.  Returns (losses, seconds generating, seconds
+    training)."""
+    import time
+
+    lr_end = lr / 20 if lr_end is None else lr_end
+    seeds = list(seeds)
+    steps = (len(seeds) + batch - 1) // batch
+    losses, t_gen, t_train, step, inb = [], 0.0, 0.0, 0, 0
+    for i, sd in enumerate(seeds):
+        t0 = time.perf_counter()
+        b, p, mask, _ = training_pair(grid, sd, dt, solver)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        losses.append(net.accumulate(grid, b, p, dt))
+        inb += 1
+        if inb == batch or i == len(seeds) - 1:
+            t = step / max(1, steps - 1)
+            net.adam_step(lr=lr_end + 0.5 * (lr - lr_end) * (1 + np.cos(np.pi * t)), grad_scale=1.0 / inb)
+            step += 1
+            inb = 0
+        torch.cuda.synchronize()
+        t_gen += t1 - t0
+        t_train += time.perf_counter() - t1
+        if log and (i + 1) % 500 == 0:
+            log("pair %d loss %.4g" % (i + 1, float(np.mean(losses[-500:]))))
+    return losses, t_gen, t_train
+
+
 __all__ = ["PressureNet", "he_init", "num_params", "solve_with_guess", "training_pair", "box_obstacles",
-           "noise_velocity", "estimate_out_scale", "train", "Simplex2"]
+           "noise_velocity", "estimate_out_scale", "train", "train_streaming", "Simplex2"]

@@ -81,10 +81,31 @@ WORKLOADS = {
     # 3D MAC grid 256^3, filtered-noise velocity (max |u| = 2 cells/step, so
     # dt = 1), walls, one step of trilinear advection + 7-point projection
     # to relative residual 1e-6.
-    "precision_3d_256": dict(dims=(256, 256, 256), dt=1.0, rel_tol=1e-6, buoyancy=0.0),
+    "precision_3d_256": dict(dims=(256, 256, 256), dt=1.0, rel_tol=1e-6, buoyancy=0.0, cpu=True, compare="plain"),
     # 2D plume 256^2: blob at (0.5, 0.15), sigma 0.04, buoyancy 1, dt 0.5, 1e-5.
-    "plume_2d_256": dict(dims=(256, 256), dt=0.5, rel_tol=1e-5, buoyancy=1.0),
+    "plume_2d_256": dict(dims=(256, 256), dt=0.5, rel_tol=1e-5, buoyancy=1.0, cpu=True, compare="plain"),
+    # Large single grid 512^3: solid sphere r = 64 at the centre, smoke from a
+    # bottom-centre disk of radius 32 (density 1), buoyancy 1, velocity from
+    # rest, trilinear advection, projection to 1e-6 by MG-PCG (chosen) and by
+    # Jacobi-PCG (the comparison).
+    "sphere_3d_512": dict(dims=(512, 512, 512), dt=0.5, rel_tol=1e-6, buoyancy=1.0, cpu=False, compare="jacobi",
+                          sphere_r=64, disk_r=32),
 }
+
+
+def sphere_plume(dims, sphere_r=64, disk_r=32, disk_h=4):
+    """Cell mask of a solid sphere at the centre and the source field of a
+    smoke disk (density 1) on the bottom (y = 0 side), both centred in x
+    and z; radii and thickness scale with min(dims) / 512."""
+    d, h, w = dims
+    sc = min(dims) / 512.0
+    z, y, x = np.ogrid[0:d, 0:h, 0:w]
+    zc, yc, xc = z + 0.5 - d / 2, y + 0.5 - h / 2, x + 0.5 - w / 2
+    r = sphere_r * sc
+    mask = ((zc * zc + yc * yc + xc * xc) < r * r).astype(np.uint8)
+    rd = disk_r * sc
+    src = (((zc * zc + xc * xc) < rd * rd) & (y < max(1, int(round(disk_h * max(sc, 0.25)))))).astype(np.float32)
+    return mask, np.broadcast_to(src, dims).astype(np.float32)
 
 
 def batch_grids(count=512, seed=3, sides=tuple(range(64, 513, 32)), max_circles=8, rmin=4, rmax=32, sigma=4.0):
@@ -121,6 +142,8 @@ def initial_state(name, dims=None):
     """(vel, density) host arrays for a named workload (dims overridable)."""
     spec = WORKLOADS[name]
     dims = tuple(dims or spec["dims"])
+    if name.startswith("sphere_3d"):
+        return np.zeros(num_faces(dims), np.float32), np.zeros(dims, np.float32)
     if name.startswith("plume_2d"):
         vel = np.zeros(num_faces(dims), np.float32)
         rho = gaussian_blob_2d(dims)
