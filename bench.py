@@ -43,7 +43,7 @@ METRIC = "Mcell-steps/s at rel. residual 1e-6 on 1 GB300; chosen form vs plain F
 UNIT = "Mcell-steps/s"
 
 # Algorithmic bytes per cell for one launch of each kernel kind (f32 fields,
-# uint8 face-open flags), 3D / 2D.  See the design doc for the derivations.
+# uint8 face-open flags), 3D / 2D: the unique bytes each launch must move.
 BYTES_PER_CELL = {
     "cg_spmv": (17, 17),        # r, p_old, flags in; p_new, Ap out
     "cg_update": (24, 24),      # x, p, r, Ap in; x, r out (Jacobi: +1 flags)
