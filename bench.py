@@ -645,9 +645,10 @@ def bench_learned(args):
 def bench_batch(args):
     """512 2D grids, sides from {64, 96, ..., 512}, 0-8 solid circles, a
     Gaussian source at a boundary-adjacent cell, dt 0.5, buoyancy 1; every
-    stage one launch over all grids (the batch path), Jacobi-PCG to relative
-    1e-6 per grid; tile shape from the autotuner.  Grids are partitioned by
-    cost across ranks (no data exchange)."""
+    stage one launch over all grids (the batch path), batched MG-PCG to
+    relative 1e-6 per grid (batched Jacobi-PCG beside it); tile shape from
+    the autotuner.  Grids are partitioned by cost across ranks (no data
+    exchange)."""
     import torch
 
     import panopaea_gb300 as pg
@@ -667,9 +668,12 @@ def bench_batch(args):
     t_tune = time.time() - t0
     v, rho, p = B.new_faces(), B.new_cells(), B.new_cells()
     src = torch.from_numpy(B.pack_cells([srcs_all[i] for i in part])).cuda()
-    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
-                        zero_solid_after_project=True,
-                        solver=pg.SolverConfig(precond=1, rel_stop=True, rel_tol=1e-6, max_iter=100000))
+    def cfg_for(precond):
+        return pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                             zero_solid_after_project=True,
+                             solver=pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=1e-6, max_iter=100000))
+
+    cfg = cfg_for(2)
     for _ in range(args.warmup):
         B.step(cfg, v, rho, p, source_field=src)
     stream = torch.cuda.current_stream()
@@ -690,19 +694,63 @@ def bench_batch(args):
     total_cells = sum(h * w for h, w in dims_all)
     value = total_cells * args.steps / (ms / 1e3) / 1e6
     its = [max(s["iterations"] for s in st) for st in stats]
+    # profiled pass (CUDA events per launch, host-polled loop)
+    import ctypes as C
+
+    lib.pg_profile_reset()
+    lib.pg_profile_enable(1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    B.step(cfg, v, rho, p, source_field=src)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    lib.pg_profile_enable(0)
+    ms_prof = e0.elapsed_time(e1)
+    kinds = {}
+    for k in range(lib.pg_profile_num_kinds()):
+        t, n = C.c_double(), C.c_int64()
+        lib.pg_profile_read(k, C.byref(t), C.byref(n))
+        if n.value:
+            kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
+    # comparison: batched Jacobi-PCG on the same state (one step)
+    cmp = None
+    if not args.no_plain:
+        cj = cfg_for(1)
+        B.step(cj, v, rho, p, source_field=src)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st_j = B.step(cj, v, rho, p, source_field=src)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_j = dist.max(e0.elapsed_time(e1))
+        cmp = {"value": total_cells / (ms_j / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms_j,
+               "max_iterations": max(s["iterations"] for s in st_j), "speedup_of_chosen": (ms_j / (ms / args.steps))}
+    peak, peak_src = peaks()
+    roof = None
+    if "mg_smooth" in kinds:
+        tot, n = kinds["mg_smooth"]
+        achieved = BYTES_PER_CELL["mg_smooth"][1] * sum(h * w for h, w in dims) / (tot / n / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "mg_smooth", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes_per_launch": BYTES_PER_CELL["mg_smooth"][1] * sum(h * w for h, w in dims),
+                "avg_launch_ms": tot / n, "launches": n, "share_of_profiled": tot / ms_prof}
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch_512", "grids": len(dims_all), "cells": total_cells, "dt": 0.5,
-                       "rel_tol": 1e-6, "form": "batched Jacobi-PCG, one launch per stage over all grids, "
-                                                "device-side graph loop",
+                       "rel_tol": 1e-6, "form": "batched MG-PCG (one V-cycle per iteration over every grid's "
+                                                "hierarchy), one launch per stage over all grids, device-side "
+                                                "graph loop",
                        "tile": list(tile), "autotune_s": t_tune, "parallelism": "cost-partitioned x%d" % ws,
                        "l2": "fields of %.0f MB per step" % (total_cells * 4 * 6 / 1e6)},
             "max_iterations_per_step": its,
             "statuses": sorted(set(s["status"] for st in stats for s in st)),
-            "cpu_baseline": None, "roofline": None, "e2e": None, "clocks": clk, "gpu_launches": int(launches),
+            "batched_jacobi_pcg": cmp,
+            "profiled_ms_per_step": ms_prof,
+            "kernels_ms": {k: {"ms": t, "launches": n} for k, (t, n) in sorted(kinds.items(), key=lambda kv: -kv[1][0])},
+            "cpu_baseline": None, "roofline": roof, "e2e": None, "clocks": clk, "gpu_launches": int(launches),
         }
         print(json.dumps(out), flush=True)
     dist.close()

@@ -329,7 +329,8 @@ int pg_batch_set_tile(pg_batch* batch, int32_t tile_x, int32_t tile_y, int32_t f
  * keyed by device and batch shape. */
 int pg_batch_autotune(pg_batch* batch, const char* cache_path);
 /* One step of every grid.  params->source_enabled must be 0 (use
- * source_field, a packed device cell field); solver: NONE or JACOBI, no
+ * source_field, a packed device cell field); solver: NONE, JACOBI or MG (a
+ * batched multigrid V-cycle over every grid's own hierarchy), no
  * refinement.  stats: count entries (may be NULL).  Returns PG_OK, or the
  * first non-OK per-grid status. */
 int pg_batch_step_f32(pg_batch* batch, const pg_step_params* params, float* vel, float* density, float* pressure,

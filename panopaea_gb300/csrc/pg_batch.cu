@@ -22,89 +22,9 @@
 #include <string>
 #include <vector>
 
-#include "pg_cg.cuh"
-#include "pg_ops2d.cuh"
+#include "pg_batch.cuh"
 
 namespace pg {
-
-struct GInfo {
-    int h, w;
-    i64 coff, foff;     // first cell / first face of the grid in the packed fields
-    int t0, t1;         // cell-tile range [t0, t1)
-    float hix, hiy;     // n - 1.00001 rounded to float, per axis (advect clamp)
-};
-
-struct Tile {
-    int grid, y0, x0;
-};
-
-struct BState {
-    double sigma, pap, alpha, beta, rmax, bmax, thr;
-    int iter, max_iter, done, status, first, nan_seen;
-};
-
-}  // namespace pg
-
-struct pg_batch {
-    int n = 0;
-    std::vector<int> h, w;
-    std::vector<pg::i64> coff, foff;  // n + 1 entries
-    pg::i64 ncells = 0, nfaces = 0;
-    cudaStream_t stream = nullptr;
-    int device = 0, num_sms = 0;
-    // device data
-    pg::GInfo* ginfo = nullptr;
-    uint8_t* flags = nullptr;       // packed cells: face-open bits
-    uint8_t* face_solid = nullptr;  // packed faces (optional)
-    pg::BState* state = nullptr;
-    int* active = nullptr;          // grids still iterating (written by the finaliser)
-    double* partials = nullptr;     // 2 per tile
-    float *r = nullptr, *ap = nullptr, *p0 = nullptr, *p1 = nullptr, *b = nullptr, *tmp = nullptr;
-    float* vtmp = nullptr;
-    // tiling (cells) -- extended tiles cover the (h+1) x (w+1) face index box
-    int tx = 32, ty = 8, fused = 1;
-    int ntiles = 0, ntiles_ext = 0;
-    pg::Tile* tiles = nullptr;
-    pg::Tile* tiles_ext = nullptr;
-    std::vector<pg::GInfo> host_info;
-    // graph of the CG loop
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    int graph_tx = 0, graph_ty = 0, graph_fused = -1, graph_pm = -1;
-    float graph_dt = 0.f;
-    float* graph_x = nullptr;
-};
-
-namespace pg {
-
-constexpr int kBMaxThreads = 256;
-
-// Block reductions for a runtime block size (a multiple of 32, <= 256).
-__device__ __forceinline__ double bsum(double v, double* sm) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    __syncthreads();
-    if (lane == 0) sm[wid] = v;
-    __syncthreads();
-    v = (threadIdx.x < nw) ? sm[threadIdx.x] : 0.0;
-    if (wid == 0)
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ double bmaxr(double v, double* sm) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    __syncthreads();
-    if (lane == 0) sm[wid] = v;
-    __syncthreads();
-    v = (threadIdx.x < nw) ? sm[threadIdx.x] : 0.0;
-    if (wid == 0)
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-#define FOR_TILES(list, count) for (int ti = blockIdx.x; ti < (count); ti += gridDim.x)
 
 // ---------------------------------------------------------------------------
 // per-stage kernels
@@ -271,9 +191,11 @@ __global__ void k_b_cg_init(float* __restrict__ x, float* __restrict__ r, const 
 
 // One block per grid: fold the grid's tile partials (fixed order).
 // stage 0: after init; 1: after the SpMV (p.Ap); 2: after the update.
+// zbuf (stage 2): z comes from an outer preconditioner after the update,
+// so beta and sigma are set later (bmg_rz_finalize).
 template <int STAGE>
 __global__ void k_b_finalize(const GInfo* __restrict__ gi, BState* __restrict__ st, const double* __restrict__ partials,
-                             int n, double rel_tol, double thr_abs, int max_iter, int* active) {
+                             int n, double rel_tol, double thr_abs, int max_iter, int* active, int zbuf = 0) {
     __shared__ double sm[32];
     const int g = blockIdx.x;
     if (g >= n) return;
@@ -332,8 +254,10 @@ __global__ void k_b_finalize(const GInfo* __restrict__ gi, BState* __restrict__ 
             S.status = PG_OK;
             S.done = 1;
         } else {
-            S.beta = bb / S.sigma;
-            S.sigma = bb;
+            if (!zbuf) {
+                S.beta = bb / S.sigma;
+                S.sigma = bb;
+            }
             S.first = 0;
             if (S.iter >= S.max_iter) S.done = 1;
         }
@@ -494,7 +418,35 @@ static int bblocks(const pg_batch* B, int ntiles) {
     return std::max(1, std::min(ntiles, B->num_sms * 8));
 }
 
-template <int PM> static void b_iter(pg_batch* B, cudaStream_t s, float dt, float* x) {
+// One CG iteration over all grids.  PM_ZBUF: z = V(r) by the batched
+// multigrid; the SpMV and update run in their identity-preconditioner form
+// with z in place of r.
+template <int PM> static void b_iter(pg_batch* B, cudaStream_t s, float dt, float* x, int nsmooth = 2) {
+    if (PM == PM_ZBUF) {
+        const int nt = B->tx * B->ty, nb = bblocks(B, B->ntiles);
+        if (B->fused) {
+            PG_LAUNCH(KK_CG_SPMV, s,
+                      k_b_spmv<PM_NONE, 1><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
+                                                             B->ntiles, B->tx, B->ty, dt, B->state, B->partials));
+        } else {
+            PG_LAUNCH(KK_CG_SPMV, s,
+                      k_b_pupdate<PM_NONE><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->flags, B->ginfo, B->tiles, B->ntiles,
+                                                             B->tx, B->ty, dt, B->state));
+            PG_LAUNCH(KK_CG_SPMV, s,
+                      k_b_spmv<PM_NONE, 0><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
+                                                             B->ntiles, B->tx, B->ty, dt, B->state, B->partials));
+        }
+        PG_LAUNCH(KK_STEP_MISC, s,
+                  k_b_finalize<1><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n, 0.0, 0.0, 0, B->active));
+        PG_LAUNCH(KK_CG_UPDATE, s,
+                  k_b_update<PM_NONE><<<nb, nt, 0, s>>>(x, B->r, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
+                                                        B->ntiles, B->tx, B->ty, dt, B->state, B->partials));
+        PG_LAUNCH(KK_STEP_MISC, s,
+                  k_b_finalize<2><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n, 0.0, 0.0, 0, B->active, 1));
+        bmg_vcycle(B, s, nsmooth);
+        bmg_rz_finalize(B, s, 0);
+        return;
+    }
     const int nt = B->tx * B->ty, nb = bblocks(B, B->ntiles);
     if (B->fused) {
         PG_LAUNCH(KK_CG_SPMV, s,
@@ -517,9 +469,10 @@ template <int PM> static void b_iter(pg_batch* B, cudaStream_t s, float dt, floa
               k_b_finalize<2><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n, 0.0, 0.0, 0, B->active));
 }
 
-template <int PM> static int b_graph(pg_batch* B, float dt, float* x) {
+template <int PM> static int b_graph(pg_batch* B, float dt, float* x, int nsmooth) {
+    const uint64_t mgkey = PM == PM_ZBUF ? (bmg_id(B) << 8) | (uint64_t)(nsmooth & 0xff) : 0;
     if (B->exec && B->graph_tx == B->tx && B->graph_ty == B->ty && B->graph_fused == B->fused &&
-        B->graph_pm == PM && B->graph_dt == dt && B->graph_x == x)
+        B->graph_pm == PM && B->graph_dt == dt && B->graph_x == x && B->graph_mg == mgkey)
         return PG_OK;
     if (B->exec) cudaGraphExecDestroy(B->exec);
     if (B->graph) cudaGraphDestroy(B->graph);
@@ -541,7 +494,7 @@ template <int PM> static int b_graph(pg_batch* B, float dt, float* x) {
     cudaError_t err = cudaStreamBeginCaptureToGraph(cs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                     cudaStreamCaptureModeThreadLocal);
     if (err == cudaSuccess) {
-        b_iter<PM>(B, cs, dt, x);
+        b_iter<PM>(B, cs, dt, x, nsmooth);
         k_b_cond<<<1, 1, 0, cs>>>(B->active, h);
         cudaGraph_t g2 = nullptr;
         err = cudaStreamEndCapture(cs, &g2);
@@ -556,6 +509,7 @@ template <int PM> static int b_graph(pg_batch* B, float dt, float* x) {
     B->graph_pm = PM;
     B->graph_dt = dt;
     B->graph_x = x;
+    B->graph_mg = mgkey;
     return PG_OK;
 }
 
@@ -564,17 +518,23 @@ template <int PM>
 static int b_solve(pg_batch* B, const pg_solver_params* prm, float dt, float* x, int max_host_iters) {
     cudaStream_t s = B->stream;
     const int nt = B->tx * B->ty, nb = bblocks(B, B->ntiles);
+    const int nsmooth = prm->mg_smooth > 0 ? prm->mg_smooth : 2;
+    constexpr int PMI = PM == PM_ZBUF ? PM_NONE : PM;  // init: r = b (z comes from the V-cycle)
     PG_CUDA(cudaMemsetAsync(B->active, 0, sizeof(int), s));
     PG_LAUNCH(KK_CG_INIT, s,
-              k_b_cg_init<PM><<<nb, nt, 0, s>>>(x, B->r, B->b, B->flags, B->ginfo, B->tiles, B->ntiles, B->tx, B->ty,
-                                                dt, B->partials));
+              k_b_cg_init<PMI><<<nb, nt, 0, s>>>(x, B->r, B->b, B->flags, B->ginfo, B->tiles, B->ntiles, B->tx, B->ty,
+                                                 dt, B->partials));
     PG_LAUNCH(KK_STEP_MISC, s,
               k_b_finalize<0><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n,
                                                    prm->rel_stop ? prm->rel_tol : 0.0, prm->threshold,
                                                    (int)std::min<i64>(prm->max_iter, 1 << 30), B->active));
+    if (PM == PM_ZBUF) {
+        bmg_vcycle(B, s, nsmooth);
+        bmg_rz_finalize(B, s, 1);
+    }
     PG_CHECK_LAUNCH();
     if (max_host_iters < 0 && graphs_enabled()) {
-        int rc = b_graph<PM>(B, dt, x);
+        int rc = b_graph<PM>(B, dt, x, nsmooth);
         if (rc) return rc;
         PG_CUDA(cudaGraphLaunch(B->exec, s));
     } else {
@@ -583,7 +543,7 @@ static int b_solve(pg_batch* B, const pg_solver_params* prm, float dt, float* x,
         int act = 1;
         for (int it = 0; it < lim && act > 0; it += 8) {
             PG_CUDA(cudaMemsetAsync(B->active, 0, sizeof(int), s));
-            for (int k = 0; k < 8 && it + k < lim; ++k) b_iter<PM>(B, s, dt, x);
+            for (int k = 0; k < 8 && it + k < lim; ++k) b_iter<PM>(B, s, dt, x, nsmooth);
             PG_CUDA(cudaMemcpyAsync(&act, B->active, sizeof(int), cudaMemcpyDeviceToHost, s));
             PG_CUDA(cudaStreamSynchronize(s));
         }
@@ -701,8 +661,9 @@ int pg_batch_destroy(pg_batch* B) {
     cudaDeviceSynchronize();
     if (B->exec) cudaGraphExecDestroy(B->exec);
     if (B->graph) cudaGraphDestroy(B->graph);
+    bmg_release(B);
     void* ptrs[] = {B->ginfo, B->flags, B->face_solid, B->state, B->active, B->partials, B->r, B->ap, B->p0,
-                    B->p1, B->b, B->tmp, B->vtmp, B->tiles, B->tiles_ext};
+                    B->p1, B->b, B->tmp, B->vtmp, B->tiles, B->tiles_ext, B->z};
     for (void* p : ptrs) cudaFree(p);
     delete B;
     return PG_OK;
@@ -736,6 +697,7 @@ int pg_batch_set_solid_cells(pg_batch* B, const uint8_t* cs) {
         PG_CUDA(cudaFree(B->face_solid));
         B->face_solid = nullptr;
     }
+    B->mask_version += 1;
     return PG_OK;
 }
 
@@ -761,9 +723,13 @@ int pg_batch_step_f32(pg_batch* B, const pg_step_params* prm, float* vel, float*
     if (!B || !prm || !vel || !rho || !pressure) return bad_arg("pg_batch_step_f32: NULL argument");
     if (prm->source_enabled) return bad_arg("pg_batch_step_f32: use source_field for batches");
     const pg_solver_params* sp = &prm->solver;
-    if (sp->precond != PG_PRECOND_NONE && sp->precond != PG_PRECOND_JACOBI)
-        return bad_arg("pg_batch_step_f32: batches support PG_PRECOND_NONE and PG_PRECOND_JACOBI");
+    if (sp->precond != PG_PRECOND_NONE && sp->precond != PG_PRECOND_JACOBI && sp->precond != PG_PRECOND_MG)
+        return bad_arg("pg_batch_step_f32: unknown preconditioner");
     if (sp->refine > 0) return bad_arg("pg_batch_step_f32: refinement is not available for batches");
+    if (sp->precond == PG_PRECOND_MG) {
+        const int rc = bmg_ensure(B, (float)prm->dt);
+        if (rc) return rc;
+    }
     cudaStream_t s = B->stream;
     const float dt = (float)prm->dt;
     const int nt = B->tx * B->ty;
@@ -786,8 +752,9 @@ int pg_batch_step_f32(pg_batch* B, const pg_step_params* prm, float* vel, float*
               k_b_rhs<<<nbc, nt, 0, s>>>(B->b, vel, B->flags, B->face_solid, B->ginfo, B->tiles, B->ntiles, B->tx,
                                          B->ty));
     PG_CHECK_LAUNCH();
-    int rc = sp->precond == PG_PRECOND_JACOBI ? b_solve<PM_JACOBI>(B, sp, dt, pressure, -1)
-                                              : b_solve<PM_NONE>(B, sp, dt, pressure, -1);
+    int rc = sp->precond == PG_PRECOND_MG       ? b_solve<PM_ZBUF>(B, sp, dt, pressure, -1)
+             : sp->precond == PG_PRECOND_JACOBI ? b_solve<PM_JACOBI>(B, sp, dt, pressure, -1)
+                                                : b_solve<PM_NONE>(B, sp, dt, pressure, -1);
     if (rc) return rc;
     PG_LAUNCH(KK_PROJECT, s,
               k_b_project<<<nbe, nt, 0, s>>>(vel, pressure, B->flags, B->ginfo, B->tiles_ext, B->ntiles_ext, B->tx,

@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "panopaea_gpu.h"
 
@@ -192,6 +193,24 @@ void release_cg_graphs(pg_grid* g);
         __VA_ARGS__;                        \
         ::pg::prof_end((stream), (kind));   \
     } while (0)
+
+// Disconnected fluid components (pg_pocket.cu): on grids with more than one,
+// the cells of every component grouped by component and cut into chunks.
+struct Pockets {
+    int* cells = nullptr;
+    int* start = nullptr;        // ncomp + 1 offsets into cells
+    int* chunk_start = nullptr;  // nchunk + 1 offsets into cells
+    int* chunk_comp = nullptr;   // component of each chunk
+    int* comp_chunk = nullptr;   // ncomp + 1 offsets into the chunks
+    double* partials = nullptr;  // nchunk partial sums, then ncomp means
+    int ncomp = 0, nchunk = 0;
+};
+void find_pockets(const uint8_t* flags, int nd, i64 d, i64 h, i64 w, i64 base, std::vector<i64>& cells,
+                  std::vector<int>& start);
+int upload_pockets(const std::vector<i64>& cells, const std::vector<int>& start, Pockets* pk);
+void release_pockets(Pockets* pk);
+// a -= its mean over each component (stream-ordered; nothing for connected fluid)
+void pocket_project(cudaStream_t s, float* a, const Pockets& pk);
 
 int ensure_workspace(pg_grid* g);
 void release_extras(pg_grid* g);

@@ -53,6 +53,7 @@ struct MgHierarchy {
     MgLevel lv[kMaxLevels];
     void* mem = nullptr;
     uint64_t id = 0;  // unique per build (CUDA-graph cache key)
+    Pockets pockets;  // fluid components (empty when the fluid is connected)
 };
 
 static uint64_t next_hierarchy_id() {
@@ -321,6 +322,7 @@ static LV view(const MgHierarchy& H, int l) {
 
 void release_mg(Extras* ex) {
     if (ex->mg) {
+        release_pockets(&ex->mg->pockets);
         cudaFree(ex->mg->mem);
         delete ex->mg;
         ex->mg = nullptr;
@@ -382,6 +384,16 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
         p += 6 * stride;
     }
     ex->mg = H;
+    // fluid components of the mask (host labelling, once per mask)
+    {
+        std::vector<uint8_t> hf((size_t)g->dims.nc());
+        PG_CUDA(cudaMemcpy(hf.data(), g->flags, hf.size(), cudaMemcpyDeviceToHost));
+        std::vector<i64> cells;
+        std::vector<int> start;
+        find_pockets(hf.data(), g->dims.nd, g->dims.d, g->dims.h, g->dims.w, 0, cells, start);
+        int prc = upload_pockets(cells, start, &H->pockets);
+        if (prc) return prc;
+    }
     // coarse operators
     cudaStream_t s = g->stream;
     for (int l = 0; l + 1 < nl; ++l) {
@@ -437,6 +449,18 @@ static void smooth_lv(pg_grid* g, const MgHierarchy& H, int l, float* e, const f
 }
 
 // Enqueue z = V(r) on the grid's stream.
+static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, int nsmooth);
+
+// z = P V(P r): P removes the mean of every fluid component when there are
+// several (pg_pocket.cu); r is projected in place (the CG's recursive
+// residual then measures the consistent part).
+static int vcycle_projected(pg_grid* g, const MgHierarchy& H, float* r, float* z, int nsmooth) {
+    pocket_project(g->stream, r, H.pockets);
+    const int rc = vcycle(g, H, r, z, nsmooth);
+    pocket_project(g->stream, z, H.pockets);
+    return rc;
+}
+
 static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, int nsmooth) {
     cudaStream_t s = g->stream;
     const int nl = H.nlev;
@@ -507,7 +531,9 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
 struct MgHook : ZHook {
     MgHierarchy* H;
     int nsmooth;
-    int apply(pg_grid* g, const void* r, void* z) override { return vcycle(g, *H, (const float*)r, (float*)z, nsmooth); }
+    int apply(pg_grid* g, const void* r, void* z) override {
+        return vcycle_projected(g, *H, (float*)const_cast<void*>(r), (float*)z, nsmooth);
+    }
     uintptr_t key() const override { return (uintptr_t)(H->id << 8) | (uintptr_t)(nsmooth & 0xff); }
 };
 

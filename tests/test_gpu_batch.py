@@ -1,7 +1,9 @@
 """Batched 2D grids (pg_batch_*): every grid of a batch advanced in one
 launch per stage must match the same grid stepped alone -- bit for bit in
 advection, -div and projection (shared per-sample arithmetic), within CG
-rounding overall (the per-grid reductions run in a different order)."""
+rounding overall (the per-grid reductions run in a different order).  The
+batched multigrid preconditioner is checked the same way against the
+single-grid MG-PCG, and by the divergence its projection leaves."""
 
 import numpy as np
 import pytest
@@ -40,7 +42,7 @@ def config(pg, precond):
                          solver=pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=1e-5, max_iter=20000))
 
 
-@pytest.mark.parametrize("precond", [0, 1])
+@pytest.mark.parametrize("precond", [0, 1, 2])
 def test_batch_matches_single_grids(pg, precond):
     masks, vels, rhos, srcs = make_case()
     B = pg.Batch2d(DIMS)
@@ -72,7 +74,15 @@ def test_batch_matches_single_grids(pg, precond):
         assert np.abs(bv - sv).max() <= 1e-3 * scale_v, (i, h, w)
         assert np.abs(br - sr).max() <= 1e-3 * max(np.abs(sr).max(), 1e-6), (i, h, w)
         assert stats[i]["status"] == 0
-        assert abs(stats[i]["iterations"] - st1["iterations"]) <= max(3, 0.1 * st1["iterations"]), (i, stats[i], st1)
+        if precond == 2 and min(h, w) > 2 and h * w > 64:
+            # same hierarchy and V-cycle as the single-grid MG
+            assert abs(stats[i]["iterations"] - st1["iterations"]) <= 2, (i, stats[i], st1)
+        elif precond == 2:
+            # too small to coarsen: the batch solves level 0 with the coarse
+            # solver, the single grid with symmetric sweeps
+            assert stats[i]["iterations"] <= max(8, 2 * st1["iterations"]), (i, stats[i], st1)
+        else:
+            assert abs(stats[i]["iterations"] - st1["iterations"]) <= max(3, 0.1 * st1["iterations"]), (i, stats[i], st1)
 
 
 def test_batch_first_step_fields_bit_exact(pg):
@@ -94,7 +104,8 @@ def test_batch_first_step_fields_bit_exact(pg):
         assert torch.equal(B.faces_of(v, i), gv.data), i
 
 
-def test_batch_graph_loop_equals_host_loop(pg):
+@pytest.mark.parametrize("precond", [0, 2])
+def test_batch_graph_loop_equals_host_loop(pg, precond):
     lib = pg.load()
     masks, vels, rhos, srcs = make_case(2)
     outs = []
@@ -106,7 +117,7 @@ def test_batch_graph_loop_equals_host_loop(pg):
         p = B.new_cells()
         lib.pg_profile_enable(int(profiled))
         try:
-            st = B.step(config(pg, 0), v, rho, p)
+            st = B.step(config(pg, precond), v, rho, p)
         finally:
             lib.pg_profile_enable(0)
         outs.append((st, v.cpu(), p.cpu()))
@@ -144,9 +155,38 @@ def test_batch_rejections(pg):
 
     B = pg.Batch2d([(8, 8), (9, 7)])
     v, rho, p = B.new_faces(), B.new_cells(), B.new_cells()
-    for solver in (pg.SolverConfig(precond=2), pg.SolverConfig(refine=2)):
+    for solver in (pg.SolverConfig(precond=5), pg.SolverConfig(refine=2)):
         with pytest.raises(N.PgError) as ei:
             B.step(pg.StepConfig(source_enabled=False, solver=solver), v, rho, p)
         assert ei.value.status == N.PG_BAD_ARG
     with pytest.raises(N.PgError):
         pg.Batch2d([(1, 8)])
+
+
+def test_batch_mg_projection_divergence(pg, oracle):
+    """The batched multigrid configuration on 24 grids of 64..256 cells per
+    side with solid circles (several grids have isolated fluid pockets):
+    every grid converges to relative 1e-6 in a few iterations, and the
+    projected velocity's divergence (FP64, oracle operator) is below 1e-5 of
+    the right-hand side's max plus 4e-6 of max |u|: the batch solves in FP32
+    without refinement, so the FP32 rounding of the pressure and of the
+    velocity bounds what the projection can remove."""
+    from panopaea_gb300 import workloads as W
+
+    dims, masks, srcs = W.batch_grids(24, seed=11, sides=tuple(range(64, 257, 32)))
+    B = pg.Batch2d(dims)
+    B.set_solid_cells(masks)
+    v, rho, p = B.new_faces(), B.new_cells(), B.new_cells()
+    src = torch.from_numpy(B.pack_cells(srcs)).cuda()
+    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True,
+                        solver=pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=1000))
+    for _ in range(4):
+        stats = B.step(cfg, v, rho, p, source_field=src)
+    torch.cuda.synchronize()
+    for i, d in enumerate(dims):
+        assert stats[i]["status"] == 0 and stats[i]["iterations"] <= 30, (i, stats[i])
+        fs = oracle.cell_mask_to_faces(masks[i])
+        vel = B.faces_of(v, i).cpu().numpy().astype(np.float64)
+        div = oracle.divergence_rhs(vel, d, fs)
+        assert np.abs(div).max() <= 1e-5 * stats[i]["b_max"] + 4e-6 * np.abs(vel).max(), (i, d)

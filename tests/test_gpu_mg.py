@@ -151,3 +151,54 @@ def test_double_float_refinement_matches_native_fp64(pg, oracle, dims):
         res.append((xh - xh.mean(), tr))
     (xa, ta), (xb, tb) = res
     assert np.abs(xa - xb).max() <= 1e-5 * np.abs(xb).max()
+
+
+@pytest.mark.parametrize("dims", [(64, 160), (24, 40, 32)])
+def test_mg_with_isolated_pockets(pg, oracle, dims):
+    """Solid walls cutting off small fluid pockets: on a pocket the
+    right-hand side sums to zero only up to FP32 rounding, which a plain
+    V-cycle turns into a diverging search direction.  With the pocket
+    projection the MG-PCG converges in a few iterations, agrees with
+    Jacobi-PCG, and leaves a divergence-free projection, in 2D and 3D."""
+    r = rng(seed_of(dims))
+    cs = np.zeros(dims, np.uint8)
+    if len(dims) == 2:
+        cs[10:22, 20] = cs[10:22, 30] = 1          # a 12 x 9 pocket
+        cs[10, 20:31] = cs[21, 20:31] = 1
+        cs[40, :] = 1                              # a wall cutting the grid in two
+        cs[50:53, 100:103] = 1
+    else:
+        cs[4:12, 5:15, 6:16] = 1                   # a hollow box: its inside is a pocket
+        cs[5:11, 6:14, 7:15] = 0
+        cs[:, 30, :] = 1                           # a wall cutting the grid in two
+    fs = oracle.cell_mask_to_faces(cs)
+    g = make_grid(pg, dims)
+    g.set_solid_cells(cs)
+    nf = oracle.num_faces(dims)
+    vel = oracle.mask_faces(oracle.walls(r.standard_normal(nf), dims), fs).astype(np.float32)
+    b = oracle.divergence_rhs(vel.astype(np.float64), dims, fs).astype(np.float32)
+    out = {}
+    for precond in (1, 2):
+        x = g.new_simplex_2()
+        st = pg.solve_pressure(g, x, cells(pg, g, b), 1.0,
+                               pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4))
+        assert st["status"] == 0, (precond, st)
+        assert st["true_residual_max"] <= 1e-6 * st["b_max"]
+        out[precond] = (st, host(x).astype(np.float64))
+    assert out[2][0]["iterations"] <= 40
+    # the solutions agree up to a constant per fluid component: compare gradients
+    ga = oracle.mask_faces(oracle.derivative_0_dual(out[1][1], dims), fs)
+    gb = oracle.mask_faces(oracle.derivative_0_dual(out[2][1], dims), fs)
+    assert np.abs(ga - gb).max() <= 1e-4 * np.abs(ga).max()
+    # the whole step on the same mask with MG stays finite and divergence-free
+    gv = faces(pg, g, vel)
+    gr, gp = cells(pg, g, r.random(dims).astype(np.float32)), g.new_simplex_2()
+    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True,
+                        solver=pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4))
+    for _ in range(4):
+        st = pg.step(g, cfg, gv, gr, gp)
+        assert st["status"] == 0
+    v = host(gv).astype(np.float64)
+    assert np.isfinite(v).all()
+    assert np.abs(oracle.divergence_rhs(v, dims, fs)).max() <= 1e-5 * st["b_max"] + 1e-6 * np.abs(v).max()
