@@ -73,6 +73,7 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-PCG comparison (profiling runs)")
     ap.add_argument("--cpu-cap", type=int, default=16, help="CG iterations per CPU sample")
+    ap.add_argument("--no-precision", action="store_true", help="skip the FP64 / BF16 precision study")
     ap.add_argument("--pairs", type=int, default=1000, help="learned_3d_128: training pairs (streamed)")
     ap.add_argument("--held", type=int, default=32, help="learned_3d_128: held-out grids")
     ap.add_argument("--gen", default="mg", choices=["mg", "plain"], help="learned_3d_128: solver of the pairs")
@@ -310,6 +311,47 @@ def reference_arm(args, spec, dims):
 
 # ---------------------------------------------------------------------------
 
+def precision_study(torch, pg, grid, spec, vel0, rho0, chosen, src):
+    """One step from the initial state three ways: the chosen FP32 form, the
+    same with the density stored in BF16, and an all-FP64 step (FP64 fields,
+    FP64 Jacobi-PCG to relative 1e-10).  Relative L-inf differences of
+    velocity and density against FP64, and each form's device time."""
+    def one(vel_t, rho_t, cfg):
+        gv, gr = pg.Simplex1(grid, vel_t.clone()), pg.Simplex2(grid, rho_t.clone())
+        gp = pg.Simplex2(grid, torch.zeros(rho_t.shape, dtype=vel_t.dtype, device="cuda"))
+        pg.step(grid, cfg, gv, gr, gp)  # warm-up (workspaces, graphs), then the same state again
+        gv.data.copy_(vel_t)
+        gr.data.copy_(rho_t)
+        gp.data.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        st = pg.step(grid, cfg, gv, gr, gp)
+        e1.record()
+        torch.cuda.synchronize()
+        return gv.data.double(), gr.data.double(), st, e0.elapsed_time(e1)
+
+    def rel(a, b):
+        return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+
+    cfg32 = step_cfg(pg, spec, chosen, src)
+    v32, r32, s32, t32 = one(torch.from_numpy(vel0).cuda(), torch.from_numpy(rho0).reshape(grid.dim()).cuda(), cfg32)
+    vb, rb, sb, tb = one(torch.from_numpy(vel0).cuda(), torch.from_numpy(rho0).reshape(grid.dim()).cuda().to(torch.bfloat16), cfg32)
+    s64 = pg.SolverConfig(precond=1, rel_stop=True, rel_tol=1e-10, max_iter=200000)
+    cfg64 = step_cfg(pg, spec, s64, None)
+    v64, r64, st64, t64 = one(torch.from_numpy(vel0).double().cuda(), torch.from_numpy(rho0).reshape(grid.dim()).double().cuda(), cfg64)
+    return {
+        "step": "one step from the initial state",
+        "fp64_reference": {"form": "FP64 fields, FP64 Jacobi-PCG to relative 1e-10", "ms": t64,
+                           "iterations": st64["iterations"]},
+        "fp32_refined": {"velocity_rel_linf_vs_fp64": rel(v32, v64), "density_rel_linf_vs_fp64": rel(r32, r64),
+                         "ms": t32, "iterations": s32["iterations"],
+                         "true_residual_rel": s32["true_residual_max"] / s32["b_max"] if s32["b_max"] else 0.0},
+        "bf16_density": {"velocity_rel_linf_vs_fp64": rel(vb, v64), "density_rel_linf_vs_fp64": rel(rb, r64),
+                         "density_rel_linf_vs_fp32": rel(rb, r32), "ms": tb, "iterations": sb["iterations"]},
+    }
+
+
 def timed_steps(torch, pg, dist, grid, cfg, gv, gr, gp, k):
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -397,6 +439,11 @@ def ours(args, spec, dims):
         plain_out = {"value": value_plain, "unit": UNIT, "ms_per_step": ms_p / kp,
                      "iterations_per_step": [s["iterations"] for s in st_p], "speedup_of_chosen": value / value_plain}
         del gv2, gr2, gp2
+    # --- precision study (256^3): FP32 storage + refinement and BF16-stored
+    # density against an all-FP64 step on the same initial state -----------
+    precision = None
+    if not args.no_precision and spec.get("cpu") and len(dims) == 3:
+        precision = precision_study(torch, pg, grid, spec, vel0, rho0, chosen, src)
     # --- e2e through the public API with host buffers ---------------------
     e2e = None
     if not args.no_e2e:
@@ -463,6 +510,7 @@ def ours(args, spec, dims):
             "iterations_per_step": its,
             "true_residual_rel": [s["true_residual_max"] / s["b_max"] if s["b_max"] else 0.0 for s in stats],
             compare_key: plain_out,
+            "precision_study": precision,
             "roofline": roof,
             "profiled_ms_per_step": ms_prof / args.steps,
             "kernels_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in sorted(kinds.items(), key=lambda kv: -kv[1][0])},

@@ -337,6 +337,20 @@ int pg_batch_step_f32(pg_batch* batch, const pg_step_params* params, float* vel,
                       pg_pcg_stats* stats);
 
 /* ----------------------------------------------------------------------- */
+/* BF16-stored density (extension; the reference's density is a Simplex2 of
+ * f64, examples/dec_fluid.rs:34-37).  Density values are bfloat16 bit
+ * patterns; every stage reads them exactly into FP32, computes as the FP32
+ * kernels do and rounds to nearest even on store.  Velocity, pressure and the
+ * solve are FP32 (with the solver's refinement options). */
+
+/* advect (dec_fluid.rs:173-211) of a BF16 cell field with FP32 velocity. */
+int pg_advect_bf16(const pg_grid* grid, uint16_t* dst, const uint16_t* src, double timestep, const float* vel);
+/* pg_step_f32 with the density stored in BF16 (advect_scheme must be 0);
+ * source_field, when set, is an FP32 device cell field. */
+int pg_step_bf16rho_f32(const pg_grid* grid, const pg_step_params* params, float* vel, uint16_t* density,
+                        float* pressure, pg_pcg_stats* stats);
+
+/* ----------------------------------------------------------------------- */
 /* Learned pressure guess (extension, no reference counterpart: panopaea has
  * no learned component).  A 3-level 3D conv U-Net, 16 base channels, BF16
  * weights and activations with FP32 accumulation on the tensor cores, trained

@@ -589,7 +589,24 @@ struct pgo_step_params {
     double threshold, rel_tol;
     long max_iter;
     int advect_scheme;           // density: 0 first order (reference), 1 MacCormack, 2 BFECC (extensions)
+    int density_bf16;            // extension: density stored in bfloat16 (rounded after every write)
 };
+
+// Round to the nearest bfloat16 (ties to even) and back: the storage rule of
+// the BF16 density.  NaN stays NaN, infinities stay.
+static float round_bf16(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u) {
+        if (u & 0x007fffffu) u |= 0x00400000u;
+    } else {
+        u += 0x7fffu + ((u >> 16) & 1u);
+    }
+    u &= 0xffff0000u;
+    std::memcpy(&x, &u, 4);
+    return x;
+}
+static double round_bf16(double x) { return (double)round_bf16((float)x); }
 
 template <class T> static void advect2(T* dst, const T* q, T dt, const T* vel, int scheme, const Shape& s);
 
@@ -639,13 +656,16 @@ void step(const Shape& s, T* vel, T* density, T* pressure, const uint8_t* fs, co
         for (idx z = prm.source_lo[0]; z < prm.source_hi[0]; ++z)
             for (idx y = prm.source_lo[1]; y < prm.source_hi[1]; ++y)
                 for (idx x = prm.source_lo[2]; x < prm.source_hi[2]; ++x) {
-                    density[(z * s.h + y) * s.w + x] = (T)prm.source_density;
+                    density[(z * s.h + y) * s.w + x] =
+                        prm.density_bf16 ? (T)round_bf16((T)prm.source_density) : (T)prm.source_density;
                     vel[vy_face_index(s, z, y, x)] = (T)prm.source_vy;
                 }
     }
     if (prm.source_field) {
         const T* sf = (const T*)prm.source_field;
         for (idx i = 0; i < nc; ++i) density[i] = rmax(density[i], sf[i]);
+        if (prm.density_bf16)
+            for (idx i = 0; i < nc; ++i) density[i] = round_bf16(density[i]);
     }
     std::vector<T> temp(nc), vel_temp(nf);
     if (s.nd == 2) {
@@ -657,6 +677,8 @@ void step(const Shape& s, T* vel, T* density, T* pressure, const uint8_t* fs, co
         advect_mac_3d(vel_temp.data(), vel, dt, vel, g);
     }
     if (prm.advect_scheme) advect2(temp.data(), density, dt, vel, prm.advect_scheme, s);
+    if (prm.density_bf16)
+        for (idx i = 0; i < nc; ++i) temp[i] = round_bf16(temp[i]);
     std::memcpy(density, temp.data(), sizeof(T) * nc);
     std::memcpy(vel, vel_temp.data(), sizeof(T) * nf);
     if (prm.walls_after_advect) walls(vel, s);
@@ -859,6 +881,29 @@ template <class T> static void advect2(T* dst, const T* q, T dt, const T* vel, i
         advect2(dst, src, (T)dt, vel, scheme, shape_of(nd, d, h, w));                                          \
     }
 PGO_BOTH(PGO_ADV2)
+
+// advect of a bfloat16 cell field (bit patterns) with a float velocity: the
+// float advection of the exactly widened values, rounded to bfloat16.
+PGO_EXPORT void pgo_advect_bf16(uint16_t* dst, const uint16_t* src, double dt, const float* vel, int nd, long d, long h,
+                                long w) {
+    const Shape s = shape_of(nd, d, h, w);
+    const idx n = s.nc();
+    std::vector<float> q(n), out(n);
+    for (idx i = 0; i < n; ++i) {
+        const uint32_t u = (uint32_t)src[i] << 16;
+        std::memcpy(&q[i], &u, 4);
+    }
+    if (nd == 2)
+        advect_2d(out.data(), q.data(), (float)dt, vel, s.h, s.w);
+    else
+        advect_3d(out.data(), q.data(), (float)dt, vel, D3{s.d, s.h, s.w});
+    for (idx i = 0; i < n; ++i) {
+        const float r = round_bf16(out[i]);
+        uint32_t u;
+        std::memcpy(&u, &r, 4);
+        dst[i] = (uint16_t)(u >> 16);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // panopaea/src/sparse.rs:119-128 SparseMatrix::mul_vec (CSR, usize indices):

@@ -36,6 +36,7 @@ class StepParams(C.Structure):
         ("rel_tol", C.c_double),
         ("max_iter", C.c_long),
         ("advect_scheme", C.c_int),
+        ("density_bf16", C.c_int),
     ]
 
 
@@ -208,7 +209,7 @@ def step(vel, density, pressure, dims, params, face_solid=None):
 
 def step_params(dt=0.05, buoyancy=0.0, source=None, source_density=1.0, source_vy=20.0, source_field=None,
                 walls_after_advect=False, zero_solid_after_project=False, precond=0, rel_stop=False,
-                threshold=0.1, rel_tol=1e-6, max_iter=100, advect_scheme=0):
+                threshold=0.1, rel_tol=1e-6, max_iter=100, advect_scheme=0, density_bf16=False):
     """StepParams; `source` = ((z0, y0, x0), (z1, y1, x1)) or None."""
     p = StepParams()
     p.dt = dt
@@ -229,6 +230,7 @@ def step_params(dt=0.05, buoyancy=0.0, source=None, source_density=1.0, source_v
     p.rel_tol = rel_tol
     p.max_iter = max_iter
     p.advect_scheme = advect_scheme
+    p.density_bf16 = int(bool(density_bf16))
     return p
 
 
@@ -239,6 +241,27 @@ def advect2(src, dt, vel, dims, scheme):
     getattr(lib(), "pgo_advect2_" + _sfx(src))(_p(out), _p(_c(src)), C.c_double(dt), _p(_c(vel)), int(scheme), nd,
                                                C.c_long(d), C.c_long(h), C.c_long(w))
     return out
+
+
+def advect_bf16(src_bits, dt, vel, dims):
+    """advect of a bfloat16 cell field given as uint16 bit patterns with a
+    float32 velocity; returns uint16 bit patterns."""
+    nd, d, h, w = _shape(dims)
+    src_bits = np.ascontiguousarray(src_bits, np.uint16)
+    vel = np.ascontiguousarray(vel, np.float32)
+    out = np.empty_like(src_bits)
+    lib().pgo_advect_bf16(_p(out), _p(src_bits), C.c_double(dt), _p(vel), nd, C.c_long(d), C.c_long(h), C.c_long(w))
+    return out
+
+
+def bf16_bits(a):
+    """float32 array -> uint16 bfloat16 bit patterns (round to nearest even)."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    return (((u + 0x7FFF + ((u >> 16) & 1)) >> 16) & 0xFFFF).astype(np.uint16)
+
+
+def bits_to_f32(b):
+    return (np.ascontiguousarray(b, np.uint16).astype(np.uint32) << 16).view(np.float32)
 
 
 def reference_face_mask(dims, box=((70, 80), (50, 70))):

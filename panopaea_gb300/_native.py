@@ -128,6 +128,8 @@ _SIGS = {
     "pg_batch_set_tile": (_I, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "pg_batch_autotune": (_I, [_P, C.c_char_p]),
     "pg_batch_step_f32": (_I, [_P, C.POINTER(StepParams), _P, _P, _P, _P]),
+    "pg_advect_bf16": (_I, [_P, _P, _P, _D, _P]),
+    "pg_step_bf16rho_f32": (_I, [_P, C.POINTER(StepParams), _P, _P, _P, C.POINTER(PcgStats)]),
     "pg_unet_num_params": (_I64, []),
     "pg_unet_create": (_I, [_I64, _I64, _I64, C.POINTER(_P)]),
     "pg_unet_destroy": (_I, [_P]),

@@ -22,6 +22,10 @@ template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, dou
 template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src, double dt, const T* vel);
 template <class T>
 int launch_advect2(const pg_grid* g, T* dst, const T* src, double dt, const T* vel, int scheme, T* t1, T* t2);
+int launch_advect_bf16(const pg_grid* g, uint16_t* dst, const uint16_t* src, double dt, const float* vel);
+int launch_source_box_bf16(const pg_grid* g, uint16_t* rho, float* vel, const pg_step_params* prm);
+int launch_source_field_bf16(const pg_grid* g, uint16_t* rho, const float* src);
+int launch_buoyancy_bf16(const pg_grid* g, float* vel, const uint16_t* rho, double dt, double beta);
 
 // Second-order scalar advection with library-owned scratch.
 template <class T> static int advect2(pg_grid* g, T* dst, const T* src, double dt, const T* vel, int scheme) {
@@ -509,9 +513,39 @@ int solve_pressure(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, do
 }
 
 // ---------------------------------------------------------------------------
-// The step (examples/dec_fluid.rs:46-141).
-template <class T>
-int step(pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure, pg_pcg_stats* st) {
+// The step (examples/dec_fluid.rs:46-141).  The density is stored as T or,
+// with R = uint16_t, as BF16 (pg_bf16.cu).
+
+// density stages for R = T
+template <class T> static int density_source_box(pg_grid* g, T* rho, T* vel, const pg_step_params* prm) {
+    return launch_source_box<T>(g, rho, vel, prm);
+}
+template <class T> static int density_source_field(pg_grid* g, T* rho, const void* src) {
+    return launch_source_field<T>(g, rho, (const T*)src);
+}
+template <class T> static int density_advect(pg_grid* g, T* dst, const T* rho, double dt, const T* vel, int scheme) {
+    return scheme == 0 ? launch_advect<T>(g, dst, rho, dt, vel) : advect2<T>(g, dst, rho, dt, vel, scheme);
+}
+template <class T> static int density_buoyancy(pg_grid* g, T* vel, const T* rho, double dt, double beta) {
+    return launch_buoyancy<T>(g, vel, rho, dt, beta);
+}
+// density stages for BF16 storage (FP32 velocity)
+static int density_source_box(pg_grid* g, uint16_t* rho, float* vel, const pg_step_params* prm) {
+    return launch_source_box_bf16(g, rho, vel, prm);
+}
+static int density_source_field(pg_grid* g, uint16_t* rho, const void* src) {
+    return launch_source_field_bf16(g, rho, (const float*)src);
+}
+static int density_advect(pg_grid* g, uint16_t* dst, const uint16_t* rho, double dt, const float* vel, int scheme) {
+    if (scheme != 0) return bad_arg("BF16 density: only the reference's advection (advect_scheme 0)");
+    return launch_advect_bf16(g, dst, rho, dt, vel);
+}
+static int density_buoyancy(pg_grid* g, float* vel, const uint16_t* rho, double dt, double beta) {
+    return launch_buoyancy_bf16(g, vel, rho, dt, beta);
+}
+
+template <class T, class R>
+int step(pg_grid* g, const pg_step_params* prm, T* vel, R* rho, T* pressure, pg_pcg_stats* st) {
     const Dims& D = g->dims;
     Extras* ex = extras_of(g);
     const size_t nc = (size_t)D.nc(), nf = (size_t)D.nf();
@@ -522,19 +556,15 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure, pg_
         return rc;
     const double dt = prm->dt;
     // inflow (dec_fluid.rs:48-57)
-    if (prm->source_enabled && (rc = launch_source_box<T>(g, rho, vel, prm))) return rc;
-    if (prm->source_field && (rc = launch_source_field<T>(g, rho, (const T*)prm->source_field))) return rc;
+    if (prm->source_enabled && (rc = density_source_box(g, rho, vel, prm))) return rc;
+    if (prm->source_field && (rc = density_source_field(g, rho, prm->source_field))) return rc;
     // advection with the old velocity (dec_fluid.rs:59-66)
-    if (prm->advect_scheme == 0) {
-        if ((rc = launch_advect<T>(g, (T*)temp, rho, dt, vel))) return rc;
-    } else if ((rc = advect2<T>(g, (T*)temp, rho, dt, vel, prm->advect_scheme))) {
-        return rc;
-    }
+    if ((rc = density_advect(g, (R*)temp, rho, dt, vel, prm->advect_scheme))) return rc;
     if ((rc = launch_advect_mac<T>(g, (T*)vtemp, vel, dt, vel))) return rc;
-    PG_CUDA(cudaMemcpyAsync(rho, temp, sizeof(T) * nc, cudaMemcpyDeviceToDevice, g->stream));
+    PG_CUDA(cudaMemcpyAsync(rho, temp, sizeof(R) * nc, cudaMemcpyDeviceToDevice, g->stream));
     PG_CUDA(cudaMemcpyAsync(vel, vtemp, sizeof(T) * nf, cudaMemcpyDeviceToDevice, g->stream));
     if (prm->walls_after_advect && (rc = launch_walls<T>(g, vel))) return rc;
-    if (prm->buoyancy != 0.0 && (rc = launch_buoyancy<T>(g, vel, rho, dt, prm->buoyancy))) return rc;
+    if (prm->buoyancy != 0.0 && (rc = density_buoyancy(g, vel, rho, dt, prm->buoyancy))) return rc;
     // -div (dec_fluid.rs:68-83)
     if ((rc = launch_rhs<T>(g, (T*)b, vel))) return rc;
     // pressure solve (dec_fluid.rs:87-121)
@@ -586,8 +616,14 @@ PG_ADV2_ABI(double, f64)
     extern "C" int pg_step_##SFX(const pg_grid* g, const pg_step_params* prm, T* vel, T* rho, T* pressure,     \
                                  pg_pcg_stats* st) {                                                           \
         if (!g || !prm || !vel || !rho || !pressure) return bad_arg("pg_step: NULL argument");                 \
-        return step<T>(const_cast<pg_grid*>(g), prm, vel, rho, pressure, st);                                  \
+        return step<T, T>(const_cast<pg_grid*>(g), prm, vel, rho, pressure, st);                               \
     }
 
 PG_STEP_ABI(float, f32)
 PG_STEP_ABI(double, f64)
+
+extern "C" int pg_step_bf16rho_f32(const pg_grid* g, const pg_step_params* prm, float* vel, uint16_t* rho,
+                                   float* pressure, pg_pcg_stats* st) {
+    if (!g || !prm || !vel || !rho || !pressure) return bad_arg("pg_step_bf16rho_f32: NULL argument");
+    return step<float, uint16_t>(const_cast<pg_grid*>(g), prm, vel, rho, pressure, st);
+}

@@ -11,6 +11,8 @@
 import ctypes as C
 from dataclasses import dataclass, field
 
+import torch
+
 from . import _native as N
 from .grid import _ptr, _sfx
 
@@ -115,9 +117,18 @@ def solve_pressure(grid, x, b, timestep, solver):
 
 
 def step(grid, config, vel, density, pressure):
-    """One fluid step in place; returns the pressure-solve statistics."""
+    """One fluid step in place; returns the pressure-solve statistics.  A
+    bfloat16 density field selects the BF16-stored density step (FP32
+    velocity and pressure)."""
     st = N.PcgStats()
     prm = config.to_c()
-    grid._call("pg_step_" + _sfx(vel.data), C.byref(prm), _ptr(vel.data), _ptr(density.data), _ptr(pressure.data),
+    name = "pg_step_bf16rho_f32" if density.data.dtype == torch.bfloat16 else "pg_step_" + _sfx(vel.data)
+    grid._call(name, C.byref(prm), _ptr(vel.data), _ptr(density.data), _ptr(pressure.data),
                C.byref(st), allow=(N.PG_OK, N.PG_NOT_CONVERGED))
     return st.as_dict()
+
+
+def advect_bf16(dst, src, timestep, vel):
+    """advect of a bfloat16 cell field with an FP32 velocity."""
+    g = src.grid
+    g._call("pg_advect_bf16", _ptr(dst.data), _ptr(src.data), C.c_double(timestep), _ptr(vel.data))
