@@ -9,7 +9,7 @@
 // the children's residuals, prolongation adds the parent's correction;
 // red-black Gauss-Seidel, `nsmooth` sweeps (red, black) before and (black,
 // red) after, so the V-cycle is symmetric; the coarsest level is solved in
-// shared memory with 32 + 32 symmetric sweeps.  Grids have different depths:
+// shared memory by symmetric sweeps.  Grids have different depths:
 // level l of the batch packs level l of every grid deep enough, each stage
 // is ONE launch over a tile list of that level (smoothing tiles of 64 x 8
 // cells, two cells of one colour per thread; restriction tiles of 32 x 8
@@ -196,8 +196,8 @@ __global__ void __launch_bounds__(kRtX * kRtY)
     }
 }
 
-// Each grid's coarsest level: one block per grid, shared memory, 32 (red,
-// black) then 32 (black, red) sweeps from e = 0.  A grid too small to
+// Each grid's coarsest level: one block per grid, shared memory, symmetric
+// red-black sweeps from e = 0 (coarse_pairs of its shape).  A grid too small to
 // coarsen is solved this way on level 0 (weights from its flags).
 __global__ void __launch_bounds__(kBmgCoarseThreads)
     k_bmg_coarse(const CoarseInfo* __restrict__ ci, const BState* __restrict__ st, float* __restrict__ z,
@@ -224,8 +224,9 @@ __global__ void __launch_bounds__(kBmgCoarseThreads)
         }
     }
     __syncthreads();
-    for (int it = 0; it < 128; ++it) {
-        const int color = it < 64 ? (it & 1) : ((it & 1) ^ 1);
+    const int pairs = coarse_pairs(1, C.h, C.w);
+    for (int it = 0; it < 4 * pairs; ++it) {
+        const int color = it < 2 * pairs ? (it & 1) : ((it & 1) ^ 1);
         for (int c = threadIdx.x; c < n; c += blockDim.x) {
             const int y = c / C.w, x = c - y * C.w;
             if (((x + y) & 1) != color) continue;

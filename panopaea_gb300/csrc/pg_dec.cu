@@ -143,7 +143,7 @@ __global__ void k_rhs(T* __restrict__ b, const T* __restrict__ vel, const uint8_
 // P is the pressure type: T (the reference's arithmetic), or double for a
 // float field projected with the FP64 pressure of the refined solve.
 template <class T, class P, class I>
-__global__ void k_project(T* __restrict__ vel, const P* __restrict__ p, const uint8_t* __restrict__ flags, Dims D, P dt,
+__global__ void k_project(T* vel, const T* src, const P* __restrict__ p, const uint8_t* __restrict__ flags, Dims D, P dt,
                           int zero_solid) {
     const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
     const I h = D.h, w = D.w, hw = h * w;
@@ -172,7 +172,7 @@ __global__ void k_project(T* __restrict__ vel, const P* __restrict__ p, const ui
             e = sub_rn(p[c - 1], p[c]);
             open = flags[c] & XLO;
         }
-        vel[i] = (zero_solid && !open) ? T(0) : add_rn(vel[i], (T)mul_rn(dt, e));
+        vel[i] = (zero_solid && !open) ? T(0) : add_rn(src[i], (T)mul_rn(dt, e));
     }
 }
 
@@ -265,18 +265,18 @@ template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel) {
     return PG_OK;
 }
 
-template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid) {
+template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid, const T* src) {
     const Dims& D = g->dims;
-    PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream, k_project<T, T, I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, p, g->flags, D, (T)dt, zero_solid)));
+    PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream, k_project<T, T, I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(vel, src ? src : vel, p, g->flags, D, (T)dt, zero_solid)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
 
-int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid) {
+int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid, const float* src) {
     const Dims& D = g->dims;
     PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream,
               k_project<float, double, I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
-                  vel, p, g->flags, D, dt, zero_solid)));
+                  vel, src ? src : vel, p, g->flags, D, dt, zero_solid)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -292,7 +292,7 @@ __device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl)
 }
 
 template <class I>
-__global__ void k_project_df(float* __restrict__ vel, const float* __restrict__ ph, const float* __restrict__ pl,
+__global__ void k_project_df(float* vel, const float* src, const float* __restrict__ ph, const float* __restrict__ pl,
                              const uint8_t* __restrict__ flags, Dims D, float dt, int zero_solid) {
     const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
     const I h = (I)D.h, w = (I)D.w, hw = h * w, d = (I)D.d;
@@ -323,15 +323,16 @@ __global__ void k_project_df(float* __restrict__ vel, const float* __restrict__ 
         }
         const bool open = flags[hi] & bit;
         const float e = df_diff(ph[lo], pl[lo], ph[hi], pl[hi]);  // p_lo - p_hi = -grad p
-        vel[i] = (zero_solid && !open) ? 0.f : __fadd_rn(vel[i], __fmul_rn(dt, e));
+        vel[i] = (zero_solid && !open) ? 0.f : __fadd_rn(src[i], __fmul_rn(dt, e));
     }
 }
 
-int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid) {
+int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid,
+                      const float* src) {
     const Dims& D = g->dims;
     PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream,
               k_project_df<I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
-                  vel, ph, pl, g->flags, D, (float)dt, zero_solid)));
+                  vel, src ? src : vel, ph, pl, g->flags, D, (float)dt, zero_solid)));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -381,7 +382,7 @@ template <class T> int launch_buoyancy(const pg_grid* g, T* vel, const T* rho, d
     template int launch_copy<T>(const pg_grid*, T*, const T*, i64);                    \
     template int launch_laplacian<T>(const pg_grid*, T*, const T*, double);            \
     template int launch_rhs<T>(const pg_grid*, T*, const T*);                          \
-    template int launch_project<T>(const pg_grid*, T*, const T*, double, int);         \
+    template int launch_project<T>(const pg_grid*, T*, const T*, double, int, const T*); \
     template int launch_walls<T>(const pg_grid*, T*);                                  \
     template int launch_source_box<T>(const pg_grid*, T*, T*, const pg_step_params*);  \
     template int launch_source_field<T>(const pg_grid*, T*, const T*);                 \
@@ -445,7 +446,7 @@ using namespace pg;
     }                                                                                                       \
     extern "C" int pg_project_##SFX(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid) {     \
         NEED(g && vel && p, "pg_project: NULL argument");                                                   \
-        return launch_project<T>(g, vel, p, dt, zero_solid);                                                \
+        return launch_project<T>(g, vel, p, dt, zero_solid, vel);                                           \
     }                                                                                                       \
     extern "C" int pg_walls_##SFX(const pg_grid* g, T* vel) {                                              \
         NEED(g && vel, "pg_walls: NULL argument");                                                          \

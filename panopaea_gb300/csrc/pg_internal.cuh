@@ -53,6 +53,16 @@ template <class T> __device__ __forceinline__ T lerp_ref(T a0, T a1, T s) {
     return add_rn(mul_rn(a0, sub_rn(T(1), s)), mul_rn(a1, s));
 }
 
+// Symmetric red-black Gauss-Seidel sweep pairs of a multigrid coarsest
+// level: Gauss-Seidel contracts the smoothest error by about 1 - c / s^2
+// per sweep on a level whose longest side is s, so s^2 / 2 pairs (at least
+// 4, at most 32) reduce it far below what the V-cycle needs.
+__host__ __device__ inline int coarse_pairs(int d, int h, int w) {
+    const int s = d > h ? (d > w ? d : w) : (h > w ? h : w);
+    const int p = (s * s + 1) / 2;
+    return p < 4 ? 4 : (p > 32 ? 32 : p);
+}
+
 // ---------------------------------------------------------------------------
 // Block reductions in FP64 (deterministic for a fixed launch shape).
 template <int NT> __device__ __forceinline__ double block_sum(double v, double* sm) {

@@ -14,8 +14,9 @@
 // correction.  Smoother: red-black Gauss-Seidel, `nsmooth` sweeps before
 // (red, black) and after (black, red) the coarse correction, so the V-cycle
 // is a symmetric operator and CG stays valid.  The coarsest level (at most
-// kCoarseMax cells) is solved by one block in shared memory with 32+32
-// symmetric sweeps.
+// kCoarseMax cells) is solved by one block in shared memory with symmetric
+// sweeps (coarse_pairs of its shape).  Every level of at most kTailCells
+// cells runs inside one single-block kernel (k_mg_tail).
 //
 // Fusions: the first pre-smoothing red half-sweep starts from e = 0, so red
 // values are f*invd and the black half-sweep computes them on the fly; the
@@ -33,6 +34,7 @@ constexpr int kMgThreads = 256;
 constexpr int kCoarseMax = 2048;
 constexpr int kCoarseThreads = 512;
 constexpr int kMaxLevels = 16;
+constexpr int kTailCells = 4096;  // levels at most this large run in the single-block tail
 
 struct MgLevel {
     Dims D;
@@ -54,6 +56,7 @@ struct MgHierarchy {
     void* mem = nullptr;
     uint64_t id = 0;  // unique per build (CUDA-graph cache key)
     Pockets pockets;  // fluid components (empty when the fluid is connected)
+    int tail = 0;     // first level handled by the single-block tail kernel (nlev: none)
 };
 
 static uint64_t next_hierarchy_id() {
@@ -221,8 +224,8 @@ __global__ void __launch_bounds__(kMgThreads)
     }
 }
 
-// Coarsest level: one block, shared memory, 32 (red, black) sweeps then 32
-// (black, red) sweeps from e = 0.
+// Coarsest level: one block, shared memory, `pairs` (red, black) sweeps then
+// `pairs` (black, red) sweeps from e = 0.
 __global__ void __launch_bounds__(kCoarseThreads) k_mg_coarse(LV v, float* __restrict__ e, const float* __restrict__ f,
                                                                CgState* st) {
     if (st->done) return;
@@ -237,9 +240,10 @@ __global__ void __launch_bounds__(kCoarseThreads) k_mg_coarse(LV v, float* __res
         si[c] = v.invd[c];
     }
     __syncthreads();
-    for (int it = 0; it < 128; ++it) {
-        // colours: 0,1 repeated 32 times, then 1,0 repeated 32 times
-        const int color = it < 64 ? (it & 1) : ((it & 1) ^ 1);
+    const int pairs = coarse_pairs(v.d, v.h, v.w);
+    for (int it = 0; it < 4 * pairs; ++it) {
+        // colours: (0, 1) `pairs` times, then (1, 0) `pairs` times
+        const int color = it < 2 * pairs ? (it & 1) : ((it & 1) ^ 1);
         for (int c = threadIdx.x; c < n; c += blockDim.x) {
             const int zy = c / v.w, x = c - zy * v.w;
             const int z = zy / v.h, y = zy - z * v.h;
@@ -258,6 +262,168 @@ __global__ void __launch_bounds__(kCoarseThreads) k_mg_coarse(LV v, float* __res
         __syncthreads();
     }
     for (int c = threadIdx.x; c < n; c += blockDim.x) e[c] = se[c];
+}
+
+// ---------------------------------------------------------------------------
+// The tail of the V-cycle: every level of at most kTailCells cells, from
+// level `lt` down to the coarsest and back, in ONE block with all level data
+// in shared memory (the same half-sweeps, restriction, coarsest solve and
+// prolongation as the per-level kernels; a block barrier replaces each
+// kernel boundary).  Input: the restricted right-hand side of level lt;
+// output: its correction e_lt, read by level lt-1's prolongation.
+
+struct TailLevel {
+    int nd, d, h, w;
+    const float* wx;
+    const float* wy;
+    const float* wz;
+    const float* invd;
+};
+
+struct TailArgs {
+    int lt, nl, nsmooth;
+    float* e_out;       // global e of level lt
+    const float* f_in;  // global f of level lt
+    TailLevel L[kMaxLevels];
+};
+
+template <int MODE>
+__device__ __forceinline__ void tail_smooth(const LV& v, float* e, const float* f, const float* ec, int cw, int ch,
+                                            int color) {
+    const int hw = v.h * v.w, half = (v.w + 1) >> 1, total = v.d * v.h * half;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        const int row = i / half, k2 = i - row * half;
+        const int z = row / v.h, y = row - z * v.h;
+        const int x = 2 * k2 + ((y + z + color) & 1);
+        if (x >= v.w) continue;
+        const int c = row * v.w + x;
+        const Cell<false> cl(v, c, z, y, x);
+        float s = f[c];
+        if (MODE == NB_SELF) {
+            e[c] = s * cl.inv;
+            continue;
+        }
+        if (cl.wxl != 0.f) s += cl.wxl * nbval<false, MODE>(v, e, f, ec, cw, ch, c - 1, z, y, x - 1);
+        if (cl.wxh != 0.f) s += cl.wxh * nbval<false, MODE>(v, e, f, ec, cw, ch, c + 1, z, y, x + 1);
+        if (cl.wyl != 0.f) s += cl.wyl * nbval<false, MODE>(v, e, f, ec, cw, ch, c - v.w, z, y - 1, x);
+        if (cl.wyh != 0.f) s += cl.wyh * nbval<false, MODE>(v, e, f, ec, cw, ch, c + v.w, z, y + 1, x);
+        if (v.nd == 3) {
+            if (cl.wzl != 0.f) s += cl.wzl * nbval<false, MODE>(v, e, f, ec, cw, ch, c - hw, z - 1, y, x);
+            if (cl.wzh != 0.f) s += cl.wzh * nbval<false, MODE>(v, e, f, ec, cw, ch, c + hw, z + 1, y, x);
+        }
+        e[c] = s * cl.inv;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void tail_restrict(const LV& v, const float* e, const float* f, float* fc, int cd, int ch,
+                                              int cw) {
+    const int hw = v.h * v.w, nc = cd * ch * cw;
+    for (int C = threadIdx.x; C < nc; C += blockDim.x) {
+        const int CZY = C / cw, X = C - CZY * cw;
+        const int Z = CZY / ch, Y = CZY - Z * ch;
+        float sum = 0.f;
+        const int z1 = v.nd == 3 ? min(2 * Z + 2, v.d) : 1;
+        const int y1 = min(2 * Y + 2, v.h), x1 = min(2 * X + 2, v.w);
+        for (int z = (v.nd == 3 ? 2 * Z : 0); z < z1; ++z)
+            for (int y = 2 * Y; y < y1; ++y)
+                for (int x = 2 * X; x < x1; ++x) {
+                    const int c = (z * v.h + y) * v.w + x;
+                    const Cell<false> cl(v, c, z, y, x);
+                    const float ecv = e[c];
+                    float a = 0.f;
+                    if (cl.wxl != 0.f) a += cl.wxl * (ecv - e[c - 1]);
+                    if (cl.wxh != 0.f) a += cl.wxh * (ecv - e[c + 1]);
+                    if (cl.wyl != 0.f) a += cl.wyl * (ecv - e[c - v.w]);
+                    if (cl.wyh != 0.f) a += cl.wyh * (ecv - e[c + v.w]);
+                    if (v.nd == 3) {
+                        if (cl.wzl != 0.f) a += cl.wzl * (ecv - e[c - hw]);
+                        if (cl.wzh != 0.f) a += cl.wzh * (ecv - e[c + hw]);
+                    }
+                    sum += f[c] - a;
+                }
+        fc[C] = sum;
+    }
+    __syncthreads();
+}
+
+constexpr int kTailThreads = 1024;
+constexpr int kTailSmemMax = 220 * 1024;
+
+__global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs A, CgState* st) {
+    if (st->done) return;
+    extern __shared__ float tsm[];
+    LV v[kMaxLevels];
+    float* E[kMaxLevels];
+    float* F[kMaxLevels];
+    // carve the shared memory: wx, wy, wz, invd, e, f per level
+    float* p = tsm;
+    for (int l = A.lt; l < A.nl; ++l) {
+        const TailLevel& T = A.L[l];
+        const int n = T.d * T.h * T.w;
+        float* wx = p;
+        float* wy = p + n;
+        float* wz = p + 2 * n;
+        float* iv = p + 3 * n;
+        E[l] = p + 4 * n;
+        F[l] = p + 5 * n;
+        p += 6 * n;
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            wx[c] = T.wx[c];
+            wy[c] = T.wy[c];
+            wz[c] = T.nd == 3 ? T.wz[c] : 0.f;
+            iv[c] = T.invd[c];
+            if (l == A.lt) F[l][c] = A.f_in[c];
+        }
+        v[l].nd = T.nd;
+        v[l].d = T.d;
+        v[l].h = T.h;
+        v[l].w = T.w;
+        v[l].flags = nullptr;
+        v[l].wx = wx;
+        v[l].wy = wy;
+        v[l].wz = wz;
+        v[l].invd = iv;
+        v[l].dt = 0.f;
+    }
+    __syncthreads();
+    const int nl = A.nl, ns = A.nsmooth;
+    // down
+    for (int l = A.lt; l + 1 < nl; ++l) {
+        const LV& c = v[l + 1];
+        tail_smooth<NB_FIRST>(v[l], E[l], F[l], nullptr, c.w, c.h, 1);
+        if (ns == 1) tail_smooth<NB_SELF>(v[l], E[l], F[l], nullptr, c.w, c.h, 0);
+        for (int k = 1; k < ns; ++k) {
+            tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 0);
+            tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 1);
+        }
+        tail_restrict(v[l], E[l], F[l], F[l + 1], c.d, c.h, c.w);
+    }
+    // coarsest: symmetric red-black Gauss-Seidel from e = 0
+    {
+        const LV& cv = v[nl - 1];
+        float* e = E[nl - 1];
+        const float* f = F[nl - 1];
+        const int n = cv.d * cv.h * cv.w;
+        for (int c = threadIdx.x; c < n; c += blockDim.x) e[c] = 0.f;
+        __syncthreads();
+        const int pairs = coarse_pairs(cv.d, cv.h, cv.w);
+        for (int it = 0; it < 4 * pairs; ++it) {
+            const int color = it < 2 * pairs ? (it & 1) : ((it & 1) ^ 1);
+            tail_smooth<NB_PLAIN>(cv, e, f, nullptr, 1, 1, color);
+        }
+    }
+    // up
+    for (int l = nl - 2; l >= A.lt; --l) {
+        const LV& c = v[l + 1];
+        tail_smooth<NB_PROLONG>(v[l], E[l], F[l], E[l + 1], c.w, c.h, 1);
+        for (int k = 0; k < ns; ++k) {
+            if (k > 0) tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 1);
+            tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 0);
+        }
+    }
+    const int n0 = A.L[A.lt].d * A.L[A.lt].h * A.L[A.lt].w;
+    for (int c = threadIdx.x; c < n0; c += blockDim.x) A.e_out[c] = E[A.lt][c];
 }
 
 // Coarse face weights: half the sum of the fine weights on the coarse face.
@@ -358,6 +524,14 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
         D = C;
     }
     H->nlev = nl;
+    // The levels from the first one of at most kTailCells cells (level >= 1)
+    // down to the coarsest run as one single-block kernel in shared memory.
+    H->tail = nl;
+    for (int l = 1; l < nl; ++l)
+        if (H->lv[l].D.nc() <= kTailCells) {
+            H->tail = l;
+            break;
+        }
     if (H->lv[nl - 1].D.nc() > kCoarseMax) {
         delete H;
         return bad_arg("PG_PRECOND_MG: grid shape does not coarsen to a small enough level (too anisotropic)");
@@ -480,8 +654,12 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
         PG_CHECK_LAUNCH();
         return PG_OK;
     }
+    // levels [0, top) run as per-level kernels; [top, nl) in the tail kernel
+    // (or, without a tail, the coarsest level alone in k_mg_coarse)
+    const bool tail = H.tail < nl;
+    const int top = tail ? H.tail : nl - 1;
     // down
-    for (int l = 0; l + 1 < nl; ++l) {
+    for (int l = 0; l < top; ++l) {
         float* e = E(l);
         const float* f = F(l);
         // pre-smoothing: (red, black) x nsmooth from e = 0; the first red is implicit
@@ -505,14 +683,33 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
                                                                                   (int)C.D.h, (int)C.D.w,
                                                                                   g->ws.state));
     }
-    // coarsest
-    {
+    if (tail) {
+        TailArgs A;
+        A.lt = top;
+        A.nl = nl;
+        A.nsmooth = nsmooth;
+        A.e_out = H.lv[top].e;
+        A.f_in = H.lv[top].f;
+        size_t smem = 0;
+        for (int l = top; l < nl; ++l) {
+            const MgLevel& L = H.lv[l];
+            A.L[l] = TailLevel{L.D.nd, (int)L.D.d, (int)L.D.h, (int)L.D.w, L.wx, L.wy, L.wz, L.invd};
+            smem += 6 * sizeof(float) * (size_t)L.D.nc();
+        }
+        static bool attr = false;
+        if (!attr) {
+            PG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax));
+            attr = true;
+        }
+        if (smem > (size_t)kTailSmemMax) return bad_arg("PG_PRECOND_MG: multigrid tail does not fit in shared memory");
+        PG_LAUNCH(KK_MG_COARSE, s, k_mg_tail<<<1, kTailThreads, smem, s>>>(A, g->ws.state));
+    } else {
         const LV v = view(H, nl - 1);
         PG_LAUNCH(KK_MG_COARSE, s,
                   k_mg_coarse<<<1, kCoarseThreads, 0, s>>>(v, H.lv[nl - 1].e, H.lv[nl - 1].f, g->ws.state));
     }
     // up
-    for (int l = nl - 2; l >= 0; --l) {
+    for (int l = top - 1; l >= 0; --l) {
         float* e = E(l);
         const float* f = F(l);
         const float* ec = H.lv[l + 1].e;

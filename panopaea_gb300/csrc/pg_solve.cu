@@ -11,9 +11,12 @@ namespace pg {
 // Launchers defined in pg_dec.cu / pg_advect.cu.
 template <class T> int launch_copy(const pg_grid* g, T* out, const T* in, i64 n);
 template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel);
-template <class T> int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid);
-int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid);
-int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid);
+// Projection into vel from the velocity src (src == vel: in place).
+template <class T>
+int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid, const T* src);
+int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid, const float* src);
+int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid,
+                      const float* src);
 template <class T> int launch_walls(const pg_grid* g, T* vel);
 template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const pg_step_params* prm);
 template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* src);
@@ -560,13 +563,15 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, R* rho, T* pressure, pg_
     if (prm->source_field && (rc = density_source_field(g, rho, prm->source_field))) return rc;
     // advection with the old velocity (dec_fluid.rs:59-66)
     if ((rc = density_advect(g, (R*)temp, rho, dt, vel, prm->advect_scheme))) return rc;
-    if ((rc = launch_advect_mac<T>(g, (T*)vtemp, vel, dt, vel))) return rc;
+    // The advected velocity stays in the scratch buffer `av` until the
+    // projection writes the step's result into vel.
+    T* av = (T*)vtemp;
+    if ((rc = launch_advect_mac<T>(g, av, vel, dt, vel))) return rc;
     PG_CUDA(cudaMemcpyAsync(rho, temp, sizeof(R) * nc, cudaMemcpyDeviceToDevice, g->stream));
-    PG_CUDA(cudaMemcpyAsync(vel, vtemp, sizeof(T) * nf, cudaMemcpyDeviceToDevice, g->stream));
-    if (prm->walls_after_advect && (rc = launch_walls<T>(g, vel))) return rc;
-    if (prm->buoyancy != 0.0 && (rc = density_buoyancy(g, vel, rho, dt, prm->buoyancy))) return rc;
+    if (prm->walls_after_advect && (rc = launch_walls<T>(g, av))) return rc;
+    if (prm->buoyancy != 0.0 && (rc = density_buoyancy(g, av, rho, dt, prm->buoyancy))) return rc;
     // -div (dec_fluid.rs:68-83)
-    if ((rc = launch_rhs<T>(g, (T*)b, vel))) return rc;
+    if ((rc = launch_rhs<T>(g, (T*)b, av))) return rc;
     // pressure solve (dec_fluid.rs:87-121)
     pg_pcg_stats s{};
     if ((rc = solve_pressure<T>(g, &prm->solver, pressure, (const T*)b, dt, &s))) return rc;
@@ -576,12 +581,13 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, R* rho, T* pressure, pg_
         void* x64;
         if ((rc = ex->buffer(Extras::kX64, sizeof(double) * nc, &x64))) return rc;
         if (prm->solver.fp64_native)
-            rc = launch_project_p64(g, (float*)vel, (const double*)x64, dt, prm->zero_solid_after_project);
+            rc = launch_project_p64(g, (float*)vel, (const double*)x64, dt, prm->zero_solid_after_project,
+                                    (const float*)av);
         else
             rc = launch_project_df(g, (float*)vel, (const float*)x64, (const float*)x64 + nc, dt,
-                                   prm->zero_solid_after_project);
+                                   prm->zero_solid_after_project, (const float*)av);
         if (rc) return rc;
-    } else if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project))) {
+    } else if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project, av))) {
         return rc;
     }
     PG_CUDA(cudaStreamSynchronize(g->stream));
