@@ -87,7 +87,8 @@ typedef struct pg_solver_params {
     int32_t refine;        /* 0: one plain CG run (the reference's algorithm);
                               n > 0: up to n FP64 residual refinement rounds */
     int32_t check_every;   /* iterations between host convergence polls (0 = auto) */
-    double inner_rel_tol;  /* per-round relative tolerance with refine > 0 (0 = auto) */
+    double inner_rel_tol;  /* per-round relative tolerance with refine > 0 (0 = auto:
+                              half the outer target, at least 1e-5) */
     int32_t mg_levels;     /* MG: number of levels (0 = auto) */
     int32_t mg_smooth;     /* MG: red-black Gauss-Seidel sweeps pre and post (0 = 2) */
     int32_t fp64_native;   /* refine > 0: 0 = the FP64-class residual, pressure

@@ -443,12 +443,15 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
         if (from_b && !prm->rel_stop) {
             cfg.threshold = 0.5 * prm->threshold;
         } else {
-            // Reach half the outer target, but never ask FP32 CG for more
-            // than ~1e-5 relative per round.
-            double inner = prm->inner_rel_tol > 0 ? prm->inner_rel_tol
-                           : from_b           ? 0.5 * prm->rel_tol
-                                              : 0.5 * target / rmax;
-            cfg.rel_tol = std::min(std::max(inner, 1e-5), 0.5);
+            // Automatic: reach half the outer target, but never ask FP32 CG
+            // for more than ~1e-5 relative per round.  An explicit
+            // inner_rel_tol is taken as given.
+            if (prm->inner_rel_tol > 0) {
+                cfg.rel_tol = std::min(prm->inner_rel_tol, 0.5);
+            } else {
+                const double inner = from_b ? 0.5 * prm->rel_tol : 0.5 * target / rmax;
+                cfg.rel_tol = std::min(std::max(inner, 1e-5), 0.5);
+            }
         }
         pg_pcg_stats s{};
         if (prm->precond == PG_PRECOND_MG)

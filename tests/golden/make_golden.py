@@ -47,6 +47,34 @@ def _array_after(src, name):
     return json.loads(body)
 
 
+def write_header(json_path=None):
+    """The same vectors as a C/C++ header (grid_rs_vectors.h) for the
+    compiled API tests, generated from the committed JSON fixture."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    d = json.load(open(json_path or os.path.join(here, "grid_rs_vectors.json")))
+
+    def arr(name, ctype, rows):
+        flat = [v for row in rows for v in (row if isinstance(row, list) else [row])]
+        return "static const %s %s[%d] = {%s};\n" % (ctype, name, len(flat), ", ".join(repr(float(v)) for v in flat))
+
+    dv, lp = d["grid_2d_divergence"], d["grid_2d_laplacian"]
+    out = ["/* Golden vectors of panopaea/src/dec/grid.rs (grid_2d_divergence :428-482,\n"
+           " * grid_2d_laplacian :484-515), generated from grid_rs_vectors.json by\n"
+           " * tests/golden/make_golden.py --header.  Do not edit. */\n",
+           "#pragma once\n",
+           arr("GOLDEN_DIV_VELOCITIES_Y", "float", dv["velocities_y"]),
+           arr("GOLDEN_DIV_VELOCITIES_X", "float", dv["velocities_x"]),
+           arr("GOLDEN_DIV_REF", "float", dv["div_ref"]),
+           "static const double GOLDEN_DIV_EPS = %r;\n" % dv["eps"],
+           arr("GOLDEN_LAP_FACES_PRIMAL", "double", lp["faces_primal"]),
+           arr("GOLDEN_LAP_REF", "double", lp["laplacian_ref"]),
+           "static const double GOLDEN_LAP_EPS = %r;\n" % lp["eps"]]
+    dst = os.path.join(here, "grid_rs_vectors.h")
+    with open(dst, "w") as f:
+        f.write("".join(out))
+    print("wrote", dst)
+
+
 def main(ref_root):
     path = os.path.join(ref_root, "panopaea", "src", "dec", "grid.rs")
     src = open(path).read()
@@ -80,4 +108,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1 and sys.argv[1] == "--header":
+        write_header()
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
