@@ -352,6 +352,41 @@ int pg_step_bf16rho_f32(const pg_grid* grid, const pg_step_params* params, float
                         float* pressure, pg_pcg_stats* stats);
 
 /* ----------------------------------------------------------------------- */
+/* Wavelet and divergence-free wavelet transforms (panopaea/src/math/wavelet,
+ * mod.rs:1-451, filters of haar.rs and spline.rs; the reference marks the
+ * module as early, mostly abandoned tests -- restated as written).  FP64
+ * device arrays, row-major (h, w) in 2D; `temp` is a caller scratch array of
+ * the same size; stream may be NULL.  Every transformed length must be a
+ * multiple of 2^levels and the last level at least the filter length. */
+typedef enum pg_wavelet {
+    PG_WAVELET_HAAR = 0,    /* haar.rs */
+    PG_WAVELET_BIOR13 = 1,  /* spline.rs Bior13 */
+    PG_WAVELET_BIOR22 = 2,
+    PG_WAVELET_BIOR24 = 3,
+    PG_WAVELET_BIOR31 = 4
+} pg_wavelet;
+typedef enum pg_wavelet_mode {
+    PG_WAVELET_ISOTROPIC = 0,   /* fwt_2d_isotropic / ifwt_2d_isotropic (same filter on both axes:
+                                   fwt_2d_separate_isotropic is the same forward transform) */
+    PG_WAVELET_ANISOTROPIC = 1, /* fwt_2d_anisotropic (forward only, as in the reference) */
+    PG_WAVELET_SEPARATE = 2     /* ifwt_2d_separate_isotropic (x, then y) */
+} pg_wavelet_mode;
+/* fwt_1d / ifwt_1d (mod.rs:114-143), in place: |coarse n|detail n|detail n-1|... */
+int pg_wavelet_fwt_1d(int wavelet, double* data, int64_t n, int levels, double* temp, void* cuda_stream);
+int pg_wavelet_ifwt_1d(int wavelet, double* data, int64_t n, int levels, double* temp, void* cuda_stream);
+/* 2D forward (mod.rs:145-170, 206-231, 262-294) and inverse (mod.rs:172-204, 233-260) */
+int pg_wavelet_fwt_2d(int mode, int wavelet_x, int wavelet_y, double* data, int64_t h, int64_t w, int levels,
+                      double* temp, void* cuda_stream);
+int pg_wavelet_ifwt_2d(int mode, int wavelet_x, int wavelet_y, double* data, int64_t h, int64_t w, int levels,
+                       double* temp, void* cuda_stream);
+/* div_coeff_2d / inv_div_coeff_2d (mod.rs:296-451): the divergence / n
+ * coefficients of the wavelet coefficients of (vx, vy) and back. */
+int pg_wavelet_div_coeff_2d(int levels, const double* vx, const double* vy, double* div, double* n, int64_t h,
+                            int64_t w, void* cuda_stream);
+int pg_wavelet_inv_div_coeff_2d(int levels, const double* div, const double* n, double* vx, double* vy, int64_t h,
+                                int64_t w, void* cuda_stream);
+
+/* ----------------------------------------------------------------------- */
 /* Learned pressure guess (extension, no reference counterpart: panopaea has
  * no learned component).  A 3-level 3D conv U-Net, 16 base channels, BF16
  * weights and activations with FP32 accumulation on the tensor cores, trained

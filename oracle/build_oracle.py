@@ -1,6 +1,7 @@
 """Build recipe of the oracle (test infrastructure only): compiles
-``oracle/pg_oracle.cpp`` (the fluid path) and ``oracle/unet_oracle.cpp``
-(the learned pressure guess) with g++ into ``oracle/_build/libpg_oracle.so``.
+``oracle/pg_oracle.cpp`` (the fluid path), ``oracle/unet_oracle.cpp`` (the
+learned pressure guess) and ``oracle/wavelet_oracle.cpp`` (the wavelet
+transforms) with g++ into ``oracle/_build/libpg_oracle.so``.
 
 -ffp-contract=off keeps a*b+c unfused on every host (aarch64 gcc fuses by
 default), so float results match a sequential evaluation of the reference.
@@ -15,7 +16,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRCS = [os.path.join(HERE, "pg_oracle.cpp"), os.path.join(HERE, "unet_oracle.cpp")]
+SRCS = [os.path.join(HERE, f) for f in ("pg_oracle.cpp", "unet_oracle.cpp", "wavelet_oracle.cpp")]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpg_oracle.so")
 FLAGS = ["-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-shared"]

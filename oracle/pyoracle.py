@@ -368,3 +368,56 @@ def bf16_round(x):
     fn.restype = C.c_float
     fn.argtypes = [C.c_float]
     return np.array([fn(float(v)) for v in np.ravel(x)], np.float32).reshape(np.shape(x))
+
+
+# ---------------------------------------------------------------------------
+# Wavelet transforms (oracle/wavelet_oracle.cpp); float64 arrays, returned new.
+
+def _wcall(name, *args):
+    fn = getattr(lib(), name)
+    fn.restype = None
+    fn(*args)
+
+
+def wavelet_fwt_1d(wavelet, data, levels):
+    out = np.array(data, np.float64)
+    _wcall("wvo_fwt_1d", int(wavelet), _p(out), C.c_long(out.size), int(levels))
+    return out
+
+
+def wavelet_ifwt_1d(wavelet, data, levels):
+    out = np.array(data, np.float64)
+    _wcall("wvo_ifwt_1d", int(wavelet), _p(out), C.c_long(out.size), int(levels))
+    return out
+
+
+def wavelet_fwt_2d(mode, wx, wy, data, levels):
+    out = np.array(data, np.float64)
+    h, w = out.shape
+    _wcall("wvo_fwt_2d", int(mode), int(wx), int(wy), _p(out), C.c_long(h), C.c_long(w), int(levels))
+    return out
+
+
+def wavelet_ifwt_2d(mode, wx, wy, data, levels):
+    out = np.array(data, np.float64)
+    h, w = out.shape
+    _wcall("wvo_ifwt_2d", int(mode), int(wx), int(wy), _p(out), C.c_long(h), C.c_long(w), int(levels))
+    return out
+
+
+def wavelet_div_coeff_2d(levels, vx, vy):
+    vx = np.ascontiguousarray(vx, np.float64)
+    vy = np.ascontiguousarray(vy, np.float64)
+    dv, nn = np.zeros_like(vx), np.zeros_like(vx)
+    h, w = vx.shape
+    _wcall("wvo_div_coeff_2d", int(levels), _p(vx), _p(vy), _p(dv), _p(nn), C.c_long(h), C.c_long(w))
+    return dv, nn
+
+
+def wavelet_inv_div_coeff_2d(levels, dv, nn):
+    dv = np.ascontiguousarray(dv, np.float64)
+    nn = np.ascontiguousarray(nn, np.float64)
+    vx, vy = np.zeros_like(dv), np.zeros_like(dv)
+    h, w = dv.shape
+    _wcall("wvo_inv_div_coeff_2d", int(levels), _p(dv), _p(nn), _p(vx), _p(vy), C.c_long(h), C.c_long(w))
+    return vx, vy

@@ -130,6 +130,12 @@ _SIGS = {
     "pg_batch_step_f32": (_I, [_P, C.POINTER(StepParams), _P, _P, _P, _P]),
     "pg_advect_bf16": (_I, [_P, _P, _P, _D, _P]),
     "pg_step_bf16rho_f32": (_I, [_P, C.POINTER(StepParams), _P, _P, _P, C.POINTER(PcgStats)]),
+    "pg_wavelet_fwt_1d": (_I, [_I, _P, _I64, _I, _P, _P]),
+    "pg_wavelet_ifwt_1d": (_I, [_I, _P, _I64, _I, _P, _P]),
+    "pg_wavelet_fwt_2d": (_I, [_I, _I, _I, _P, _I64, _I64, _I, _P, _P]),
+    "pg_wavelet_ifwt_2d": (_I, [_I, _I, _I, _P, _I64, _I64, _I, _P, _P]),
+    "pg_wavelet_div_coeff_2d": (_I, [_I, _P, _P, _P, _P, _I64, _I64, _P]),
+    "pg_wavelet_inv_div_coeff_2d": (_I, [_I, _P, _P, _P, _P, _I64, _I64, _P]),
     "pg_unet_num_params": (_I64, []),
     "pg_unet_create": (_I, [_I64, _I64, _I64, C.POINTER(_P)]),
     "pg_unet_destroy": (_I, [_P]),
