@@ -56,6 +56,9 @@ BYTES_PER_CELL = {
     "refine_update": (20, 20),  # x64, d in; x64 out
     # fine-level multigrid kernels, per fine cell:
     "mg_smooth": (6.5, 6.5),    # half-sweep: f, flags of its colour, e of the other in; e of its colour out
+    # fused red-black pair (3D): e, f, flags in, e out = 13; the first pre-smoothing pair reads no e (9), the
+    # first post-smoothing one also the coarse correction (13.5): 12.125 averaged over a 2-sweep V-cycle
+    "mg_pair": (12.125, 12.125),
     "mg_restrict": (9.5, 9.5),  # e, f, flags in; coarse f (1/8 or 1/4 of the cells) out
 }
 

@@ -182,7 +182,7 @@ inline int grid_blocks(const pg_grid* g, i64 n, int threads, int per_sm = 8) {
 enum KernelKind {
     KK_CG_INIT, KK_CG_SPMV, KK_CG_UPDATE, KK_CG_TAIL, KK_ADVECT, KK_ADVECT_MAC, KK_RHS, KK_PROJECT, KK_DEC_OP,
     KK_RESIDUAL64, KK_REFINE_UPDATE, KK_MG_SMOOTH, KK_MG_RESTRICT, KK_MG_SMOOTH_C, KK_MG_RESTRICT_C, KK_MG_COARSE,
-    KK_MG_SETUP, KK_STEP_MISC, KK_UNET_CONV, KK_UNET_WGRAD, KK_UNET_MISC, KK_COUNT
+    KK_MG_SETUP, KK_STEP_MISC, KK_UNET_CONV, KK_UNET_WGRAD, KK_UNET_MISC, KK_MG_PAIR, KK_COUNT
 };
 void prof_begin(cudaStream_t s, int kind);
 void prof_end(cudaStream_t s, int kind);

@@ -25,8 +25,10 @@
 // on the fly there.  The last fine-level half-sweep writes z and reduces
 // z.r into the CG state.
 #include <algorithm>
+#include <cstdlib>
 
 #include "pg_solve.cuh"
+#include "pg_tma.cuh"
 
 namespace pg {
 
@@ -57,6 +59,19 @@ struct MgHierarchy {
     uint64_t id = 0;  // unique per build (CUDA-graph cache key)
     Pockets pockets;  // fluid components (empty when the fluid is connected)
     int tail = 0;     // first level handled by the single-block tail kernel (nlev: none)
+    // fine level of 3D grids: fused red-black pairs (k_mg_pair) ping-pong
+    // between z and e0b; tensor maps of the flags and of the vectors met
+    bool pairs = false;
+    float* e0b = nullptr;
+    CUtensorMap gmap;
+    int pair_cap = 0;  // resident k_mg_pair blocks on the device
+    struct MapEnt {
+        const void* p = nullptr;
+        int by = 0;
+        CUtensorMap m;
+    };
+    mutable MapEnt maps[6];
+    mutable int next_map = 0;
 };
 
 static uint64_t next_hierarchy_id() {
@@ -186,6 +201,224 @@ __global__ void __launch_bounds__(kMgThreads)
     if (threadIdx.x == 0) {
         st->counter[3] = 0;
         cg_finish_rz(st, rz);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused red-black pair on the fine level of 3D grids.
+//
+// One launch performs a half-sweep over colour c1 and the following
+// half-sweep over the other colour c2, reading the correction from `ein`
+// and writing both colours to `eout` (out of place: a neighbouring tile's
+// first half-sweep still needs the old c2 values this tile replaces).  A
+// block owns a kPX x kPY column tile and walks a chunk of z planes.  TMA
+// stages every plane of ein (2-cell halo), f and the face flags (1-cell
+// halo) into a kPStages-deep shared-memory ring; for plane p the block
+// computes the new c1 values on the tile plus its one-cell ring (the ring
+// cells belong to the neighbouring tiles, which compute the same values)
+// into a shared slot, then the c2 values of plane p-1 from the c1 slots of
+// planes p-2, p-1 and p, and stores both colours of plane p-1 as one float2
+// per thread.  Per cell: 4 bytes of ein, 4 of f and 1 of flags read, 4 of
+// eout written -- half the traffic of two separate half-sweeps.  The
+// arithmetic of every cell is that of k_mg_smooth<true, ...>.
+constexpr int kPX = 64, kPY = 8;
+constexpr int kPThreads = 256;  // one (c1, c2) x-pair per thread and plane
+constexpr int kPStages = 6;     // plane ring; loads run kPStages - 3 planes ahead
+constexpr int kPEw = kPX + 8, kPEh = kPY + 4;    // ein box from (x0 - 4, y0 - 2)
+constexpr int kPFw = kPX + 8, kPFh = kPY + 2;    // f box from (x0 - 4, y0 - 1)
+constexpr int kPGw = kPX + 32, kPGh = kPY + 2;   // flags box from (x0 - 16, y0 - 1)
+constexpr int kPEBytes = kPEw * kPEh * 4;        // 3456
+constexpr int kPFBytes = kPFw * kPFh * 4;        // 2880
+constexpr int kPGBytes = kPGw * kPGh;            // 960
+constexpr int kPFOff = kPEBytes;                 // every box starts on 128 bytes
+constexpr int kPGOff = kPFOff + ((kPFBytes + 127) / 128) * 128;
+constexpr int kPStageBytes = kPGOff + ((kPGBytes + 127) / 128) * 128;
+constexpr int kPSw = kPX + 2, kPSh = kPY + 2;    // new c1 values of one plane (tile + ring)
+constexpr int kPSlotBytes = kPSw * kPSh * 4;
+constexpr int kPBarOff = kPStages * kPStageBytes + 4 * kPSlotBytes;
+constexpr size_t kPSmem = 128 + kPBarOff + kPStages * 8;
+static_assert(kPEBytes % 128 == 0 && kPStageBytes % 128 == 0, "TMA boxes must stay 128-byte aligned");
+
+enum { PR_SELF = 0 /* c1 = f * invd (e = 0 before) */, PR_PLAIN = 1, PR_PROLONG = 2 /* ein + ec[parent] */ };
+
+struct PairArgs {
+    int d, h, w;
+    float dt;
+    float* eout;
+    const float* ec;  // PR_PROLONG: correction of the next coarser level
+    int cw, ch;
+    int c1;           // colour of the first half-sweep
+    int tiles_x, tiles_y, zc, nwork;
+};
+
+template <int M1, bool RZ>
+__global__ void __launch_bounds__(kPThreads)
+    k_mg_pair(const __grid_constant__ CUtensorMap emap, const __grid_constant__ CUtensorMap fmap,
+              const __grid_constant__ CUtensorMap gmap, PairArgs a, CgState* st, double* partials) {
+    if (st->done) return;
+    extern __shared__ unsigned char pair_smem_raw[];
+    __shared__ double sm[32];
+    __shared__ float inv_tab[8];  // 1 / (n dt) for n open faces (0 for n = 0), as Cell<true>
+    unsigned char* const base = (unsigned char*)(((uintptr_t)pair_smem_raw + 127) & ~(uintptr_t)127);
+    float(*const S1)[kPSh][kPSw] = (float(*)[kPSh][kPSw])(base + kPStages * kPStageBytes);
+    uint64_t* const bars = (uint64_t*)(base + kPBarOff);
+    const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
+    const float dt = a.dt;
+    if (tid == 0) {
+        for (int s = 0; s < kPStages; ++s) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+        if (M1 != PR_SELF) tma_prefetch_map(&emap);
+        tma_prefetch_map(&fmap);
+        tma_prefetch_map(&gmap);
+    }
+    if (tid < 8) inv_tab[tid] = tid ? __frcp_rn((float)tid * dt) : 0.f;
+    __syncthreads();
+    constexpr unsigned kTx = (M1 == PR_SELF ? 0 : kPEBytes) + kPFBytes + kPGBytes;
+    const int h = a.h, w = a.w, d = a.d;
+    const int per_plane = a.tiles_x * a.tiles_y;
+    auto stage = [&](unsigned j) -> const unsigned char* { return base + (j % kPStages) * kPStageBytes; };
+    auto Ev = [](const unsigned char* P, int r, int c) -> float { return ((const float*)P)[r * kPEw + c]; };
+    auto Fv = [](const unsigned char* P, int r, int c) -> float {
+        return ((const float*)(P + kPFOff))[r * kPFw + c];
+    };
+    auto Gv = [](const unsigned char* P, int r, int c) -> unsigned { return (P + kPGOff)[r * kPGw + c]; };
+    unsigned issued_end = 0;  // thread 0: one past the last plane issued
+    auto issue = [&](unsigned j, int plane, int x0, int y0) {
+        issued_end = j + 1;
+        unsigned char* dst = base + (j % kPStages) * kPStageBytes;
+        uint64_t* bar = &bars[j % kPStages];
+        mbar_expect_tx(bar, kTx);
+        if (M1 != PR_SELF) tma_load_3d(dst, &emap, bar, x0 - 4, y0 - 2, plane);
+        tma_load_3d(dst + kPFOff, &fmap, bar, x0 - 4, y0 - 1, plane);
+        tma_load_3d(dst + kPGOff, &gmap, bar, x0 - 16, y0 - 1, plane);
+    };
+    // Thread 0 alone polls the barriers; the __syncthreads that follows its
+    // wait publishes the staged plane to the block.
+    bool ok = true;
+    auto wait = [&](unsigned j) {
+        if (tid == 0 && ok) ok = mbar_wait(&bars[j % kPStages], (j / kPStages) & 1);
+    };
+    // Gauss-Seidel update from the open-face neighbour values (same
+    // operation order as k_mg_smooth<true, ...>; the loads are unconditional,
+    // every staged value is finite).
+    auto gs = [&](unsigned fl, float fv, float vxl, float vxh, float vyl, float vyh, float vzl, float vzh) -> float {
+        float s = fv;
+        s = (fl & XLO) ? fmaf(dt, vxl, s) : s;
+        s = (fl & XHI) ? fmaf(dt, vxh, s) : s;
+        s = (fl & YLO) ? fmaf(dt, vyl, s) : s;
+        s = (fl & YHI) ? fmaf(dt, vyh, s) : s;
+        s = (fl & ZLO) ? fmaf(dt, vzl, s) : s;
+        s = (fl & ZHI) ? fmaf(dt, vzh, s) : s;
+        return s * inv_tab[__popc(fl)];
+    };
+    unsigned seq = 0;     // planes this block has consumed: ring slot and phase parity
+    bool failed = false;  // block-uniform: a wait gave up
+    Acc<float> acc;
+    for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
+        const int tz = item / per_plane, t2 = item - tz * per_plane;
+        const int x0 = (t2 % a.tiles_x) * kPX, y0 = (t2 / a.tiles_x) * kPY;
+        const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
+        const int n = z1 - z0 + 4;  // planes z0 - 2 .. z1 + 1 (ring index j = plane - z0 + 2)
+        if (tid == 0)
+            for (int j = 0; j < min(n, kPStages); ++j) issue(seq + j, z0 - 2 + j, x0, y0);
+        wait(seq);
+        wait(seq + 1);
+        wait(seq + 2);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        for (int i = 0; i <= z1 - z0 + 1; ++i) {
+            const int p = z0 - 1 + i;  // plane of this step's first half-sweep
+            const unsigned char *Pm = stage(seq + i), *P0 = stage(seq + i + 1), *Pp = stage(seq + i + 2);
+            // new c1 value of cell (yl, xl) of plane p, tile coordinates
+            auto c1_cell = [&](int yl, int xl) -> float {
+                const unsigned fl = Gv(P0, yl + 1, xl + 16);
+                const float fv = Fv(P0, yl + 1, xl + 4);
+                if (M1 == PR_SELF) return fv * inv_tab[__popc(fl)];
+                if (M1 == PR_PROLONG) {  // the coarse correction only behind open faces
+                    const int gy = y0 + yl, gx = x0 + xl;
+                    auto nb = [&](float v, int z, int y, int x) -> float {
+                        return v + a.ec[((z >> 1) * a.ch + (y >> 1)) * a.cw + (x >> 1)];
+                    };
+                    float s = fv;
+                    if (fl & XLO) s += dt * nb(Ev(P0, yl + 2, xl + 3), p, gy, gx - 1);
+                    if (fl & XHI) s += dt * nb(Ev(P0, yl + 2, xl + 5), p, gy, gx + 1);
+                    if (fl & YLO) s += dt * nb(Ev(P0, yl + 1, xl + 4), p, gy - 1, gx);
+                    if (fl & YHI) s += dt * nb(Ev(P0, yl + 3, xl + 4), p, gy + 1, gx);
+                    if (fl & ZLO) s += dt * nb(Ev(Pm, yl + 2, xl + 4), p - 1, gy, gx);
+                    if (fl & ZHI) s += dt * nb(Ev(Pp, yl + 2, xl + 4), p + 1, gy, gx);
+                    return s * inv_tab[__popc(fl)];
+                }
+                return gs(fl, fv, Ev(P0, yl + 2, xl + 3), Ev(P0, yl + 2, xl + 5), Ev(P0, yl + 1, xl + 4),
+                          Ev(P0, yl + 3, xl + 4), Ev(Pm, yl + 2, xl + 4), Ev(Pp, yl + 2, xl + 4));
+            };
+            {
+                const int xl = 2 * lane + ((a.c1 + y0 + ty + p) & 1);
+                S1[p & 3][ty + 1][xl + 1] = c1_cell(ty, xl);
+            }
+            if (tid < 64) {  // ring rows y0 - 1 and y0 + kPY
+                const int yl = tid < 32 ? -1 : kPY;
+                const int xl = 2 * lane + ((a.c1 + y0 + yl + p) & 1);
+                S1[p & 3][yl + 1][xl + 1] = c1_cell(yl, xl);
+            } else if (tid < 80) {  // ring columns x0 - 1 and x0 + kPX
+                const int k = tid - 64;
+                const int xl = k < 8 ? -1 : kPX, yl = k & 7;
+                if (((x0 + xl + y0 + yl + p) & 1) == a.c1) S1[p & 3][yl + 1][xl + 1] = c1_cell(yl, xl);
+            }
+            // the next step's plane p + 2 must have landed
+            if (seq + i + 3 < seq + n) wait(seq + i + 3);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            // the ring slot of plane p - 2 is free now: load kPStages planes past it
+            if (tid == 0 && i >= 1 && i - 1 + kPStages < n) issue(seq + i - 1 + kPStages, z0 - 3 + i + kPStages, x0, y0);
+            if (i >= 2) {  // second half-sweep on plane q = p - 1, then store it
+                const int q = p - 1;
+                const int gy = y0 + ty;
+                const int xl2 = 2 * lane + ((a.c1 + 1 + gy + q) & 1), xl1 = xl2 ^ 1;
+                const float e1 = S1[q & 3][ty + 1][xl1 + 1];
+                const float fv = Fv(Pm, ty + 1, xl2 + 4);
+                const float e2 = gs(Gv(Pm, ty + 1, xl2 + 16), fv, S1[q & 3][ty + 1][xl2], S1[q & 3][ty + 1][xl2 + 2],
+                                    S1[q & 3][ty][xl2 + 1], S1[q & 3][ty + 2][xl2 + 1], S1[(q - 1) & 3][ty + 1][xl2 + 1],
+                                    S1[(q + 1) & 3][ty + 1][xl2 + 1]);
+                const int x = x0 + 2 * lane;
+                if (gy < h && x < w) {
+                    const float2 v = (xl1 & 1) ? make_float2(e2, e1) : make_float2(e1, e2);
+                    *(float2*)(a.eout + ((i64)q * h + gy) * w + x) = v;
+                    if (RZ) {
+                        acc.add(e1 * Fv(Pm, ty + 1, xl1 + 4));
+                        acc.add(e2 * fv);
+                    }
+                }
+            }
+        }
+        if (failed) break;
+        __syncthreads();  // every thread is done with the ring before the next item's loads
+        seq += n;
+    }
+    if (failed) {  // a plane never arrived: drain the copies in flight (bounded), stop the solve
+        if (tid == 0) {
+            const uint64_t t0 = global_ns();
+            for (unsigned j = issued_end > kPStages ? issued_end - kPStages : 0; j < issued_end; ++j)
+                while (!mbar_try_wait(&bars[j % kPStages], (j / kPStages) & 1) && global_ns() - t0 < kMbarWaitNs) {
+                }
+            st->status = PG_TIMEOUT;
+            st->done = 1;
+        }
+        return;
+    }
+    if (RZ) {
+        const double s = block_sum<kPThreads>(acc.value(), sm);
+        if (threadIdx.x == 0) partials[blockIdx.x] = s;
+        if (last_block(&st->counter[3])) {
+            const double rz = reduce_partials<false, kPThreads>(partials, gridDim.x, sm);
+            if (threadIdx.x == 0) {
+                st->counter[3] = 0;
+                cg_finish_rz(st, rz);
+            }
+        }
     }
 }
 
@@ -490,12 +723,15 @@ void release_mg(Extras* ex) {
     if (ex->mg) {
         release_pockets(&ex->mg->pockets);
         cudaFree(ex->mg->mem);
+        cudaFree(ex->mg->e0b);
         delete ex->mg;
         ex->mg = nullptr;
     }
 }
 
 static int blocks_for(const pg_grid* g, i64 n) { return grid_blocks(g, n, kMgThreads, 8); }
+
+static int pair_setup(pg_grid* g, MgHierarchy* H);
 
 // (Re)build the hierarchy for the grid's current mask and dt.
 static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
@@ -558,6 +794,22 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
         p += 6 * stride;
     }
     ex->mg = H;
+    // Fused fine-level pairs: 3D, rows of a multiple of 16 cells (the flags'
+    // TMA row stride), the flags' map encodable; PG_MG_PAIRS=0 keeps the
+    // separate half-sweeps (a diagnostic switch read per build).
+    {
+        const char* env = getenv("PG_MG_PAIRS");
+        const bool want = !(env && env[0] == '0');
+        const Dims& D0 = g->dims;
+        if (want && D0.nd == 3 && nl > 1 && D0.w % 16 == 0 &&
+            encode_map_3d(&H->gmap, H->flags, 1, D0.w, D0.h, D0.d, kPGw, kPGh)) {
+            err = cudaMalloc(&H->e0b, sizeof(float) * (size_t)D0.nc());
+            if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc(mg fine scratch)");
+            const int prc = pair_setup(g, H);
+            if (prc) return prc;
+            H->pairs = H->pair_cap > 0;
+        }
+    }
     // fluid components of the mask (host labelling, once per mask)
     {
         std::vector<uint8_t> hf((size_t)g->dims.nc());
@@ -588,6 +840,95 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
     PG_CHECK_LAUNCH();
     *out = H;
     return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Fused fine-level pairs: launch setup.
+
+template <int M1, bool RZ>
+static int pair_attr() {
+    return (int)cudaFuncSetAttribute(k_mg_pair<M1, RZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
+}
+
+// Opt every instantiation into its shared memory and size the grid by the
+// resident block count (outside any stream capture).
+static int pair_setup(pg_grid* g, MgHierarchy* H) {
+    int e = pair_attr<PR_SELF, false>() | pair_attr<PR_PLAIN, false>() | pair_attr<PR_PROLONG, false>() |
+            pair_attr<PR_PLAIN, true>() | pair_attr<PR_PROLONG, true>();
+    if (e) return cuda_fail((cudaError_t)e, "cudaFuncSetAttribute(k_mg_pair)");
+    int bps = 0;
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_mg_pair<PR_PLAIN, false>, kPThreads, kPSmem));
+    H->pair_cap = std::min(bps * g->num_sms, kMaxBlocks);
+    return PG_OK;
+}
+
+// Tensor map of a fine-level float vector with a box of kPEw x by, encoded
+// once per (pointer, box); nullptr when the vector cannot be mapped.
+static const CUtensorMap* vec_map(const MgHierarchy& H, const float* p, int by) {
+    for (auto& m : H.maps)
+        if (m.p == p && m.by == by) return &m.m;
+    MgHierarchy::MapEnt& m = H.maps[H.next_map];
+    const Dims& D = H.D0;
+    if (!encode_map_3d(&m.m, p, 4, D.w, D.h, D.d, kPEw, by)) return nullptr;
+    H.next_map = (H.next_map + 1) % 6;
+    m.p = p;
+    m.by = by;
+    return &m.m;
+}
+
+struct PairLaunch {
+    const CUtensorMap* fm;  // f (the residual r)
+    PairArgs a;
+    int nb;
+};
+
+// Geometry of the pair launches of one V-cycle; false when a vector cannot
+// be mapped (the V-cycle then uses the half-sweeps).
+static bool pair_plan(const MgHierarchy& H, const float* r, const float* z, PairLaunch* P) {
+    if (!H.pairs || !vec_map(H, z, kPEh) || !vec_map(H, H.e0b, kPEh) || !(P->fm = vec_map(H, r, kPFh)))
+        return false;
+    const Dims& D = H.D0;
+    PairArgs& a = P->a;
+    a.d = (int)D.d;
+    a.h = (int)D.h;
+    a.w = (int)D.w;
+    a.dt = (float)H.dt;
+    a.tiles_x = (a.w + kPX - 1) / kPX;
+    a.tiles_y = (a.h + kPY - 1) / kPY;
+    const int tiles = a.tiles_x * a.tiles_y;
+    // one work item per resident block, chunks of at least 8 planes
+    const int nch = std::max(1, std::min(H.pair_cap / tiles, (a.d + 7) / 8));
+    a.zc = (a.d + nch - 1) / nch;
+    a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
+    P->nb = std::max(1, std::min(a.nwork, H.pair_cap));
+    if (H.nlev > 1) {
+        a.cw = (int)H.lv[1].D.w;
+        a.ch = (int)H.lv[1].D.h;
+    }
+    return true;
+}
+
+template <int M1, bool RZ>
+static void pair_t(pg_grid* g, const MgHierarchy& H, const CUtensorMap* em, const PairLaunch& P, const PairArgs& a) {
+    cudaStream_t s = g->stream;
+    PG_LAUNCH(KK_MG_PAIR, s,
+              k_mg_pair<M1, RZ><<<P.nb, kPThreads, kPSmem, s>>>(*em, *P.fm, H.gmap, a, g->ws.state, g->ws.partials));
+}
+
+// One fused pair: first half-sweep over colour c1 in `mode` from ein
+// (unused for PR_SELF), second over the other colour; both into eout.
+static void pair(pg_grid* g, const MgHierarchy& H, const PairLaunch& P, int mode, int c1, bool rz, const float* ein,
+                 float* eout, const float* ec) {
+    PairArgs a = P.a;
+    a.eout = eout;
+    a.ec = ec;
+    a.c1 = c1;
+    const CUtensorMap* em = vec_map(H, ein ? ein : H.e0b, kPEh);  // cached by pair_plan
+    if (mode == PR_SELF) pair_t<PR_SELF, false>(g, H, em, P, a);
+    else if (mode == PR_PROLONG && rz) pair_t<PR_PROLONG, true>(g, H, em, P, a);
+    else if (mode == PR_PROLONG) pair_t<PR_PROLONG, false>(g, H, em, P, a);
+    else if (rz) pair_t<PR_PLAIN, true>(g, H, em, P, a);
+    else pair_t<PR_PLAIN, false>(g, H, em, P, a);
 }
 
 // Launch one half-sweep over `color` at level l.
@@ -658,16 +999,28 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
     // (or, without a tail, the coarsest level alone in k_mg_coarse)
     const bool tail = H.tail < nl;
     const int top = tail ? H.tail : nl - 1;
+    // Fine level of 3D grids as fused pairs: 2 * nsmooth of them alternate
+    // between the scratch and z (pair k writes pout[k & 1]), so the last one
+    // lands in z; the pre-smoothed correction is pout[(nsmooth - 1) & 1].
+    PairLaunch P;
+    const bool pairs = pair_plan(H, r, z, &P);
+    float* const pout[2] = {H.e0b, z};
     // down
     for (int l = 0; l < top; ++l) {
         float* e = E(l);
         const float* f = F(l);
-        // pre-smoothing: (red, black) x nsmooth from e = 0; the first red is implicit
-        smooth_lv(g, H, l, e, f, nullptr, 1, NB_FIRST);
-        if (nsmooth == 1) smooth_lv(g, H, l, e, f, nullptr, 0, NB_SELF);  // store the implicit red values
-        for (int k = 1; k < nsmooth; ++k) {
-            smooth_lv(g, H, l, e, f, nullptr, 0, NB_PLAIN);
-            smooth_lv(g, H, l, e, f, nullptr, 1, NB_PLAIN);
+        if (l == 0 && pairs) {
+            pair(g, H, P, PR_SELF, 0, false, nullptr, pout[0], nullptr);
+            for (int k = 1; k < nsmooth; ++k) pair(g, H, P, PR_PLAIN, 0, false, pout[(k - 1) & 1], pout[k & 1], nullptr);
+            e = pout[(nsmooth - 1) & 1];
+        } else {
+            // pre-smoothing: (red, black) x nsmooth from e = 0; the first red is implicit
+            smooth_lv(g, H, l, e, f, nullptr, 1, NB_FIRST);
+            if (nsmooth == 1) smooth_lv(g, H, l, e, f, nullptr, 0, NB_SELF);  // store the implicit red values
+            for (int k = 1; k < nsmooth; ++k) {
+                smooth_lv(g, H, l, e, f, nullptr, 0, NB_PLAIN);
+                smooth_lv(g, H, l, e, f, nullptr, 1, NB_PLAIN);
+            }
         }
         const LV v = view(H, l);
         const MgLevel& C = H.lv[l + 1];
@@ -713,6 +1066,12 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
         float* e = E(l);
         const float* f = F(l);
         const float* ec = H.lv[l + 1].e;
+        if (l == 0 && pairs) {
+            for (int k = nsmooth; k < 2 * nsmooth; ++k)
+                pair(g, H, P, k == nsmooth ? PR_PROLONG : PR_PLAIN, 1, k == 2 * nsmooth - 1, pout[(k - 1) & 1],
+                     pout[k & 1], k == nsmooth ? ec : nullptr);
+            continue;
+        }
         // post-smoothing: (black, red) x nsmooth; the first black reads the
         // prolonged red neighbours
         smooth_lv(g, H, l, e, f, ec, 1, NB_PROLONG);

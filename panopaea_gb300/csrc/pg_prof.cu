@@ -12,7 +12,7 @@ namespace pg {
 static const char* kKindNames[KK_COUNT] = {
     "cg_init", "cg_spmv", "cg_update", "cg_tail", "advect", "advect_mac", "rhs", "project", "dec_op",
     "residual64", "refine_update", "mg_smooth", "mg_restrict", "mg_smooth_coarse", "mg_restrict_coarse",
-    "mg_coarse", "mg_setup", "step_misc", "unet_conv", "unet_wgrad", "unet_misc",
+    "mg_coarse", "mg_setup", "step_misc", "unet_conv", "unet_wgrad", "unet_misc", "mg_pair",
 };
 
 namespace {

@@ -1,0 +1,93 @@
+// pg_tma.cuh -- tensor-memory-accelerator (TMA) plane loads and mbarrier
+// waits for the z-marching stencil kernels.
+//
+// A kernel stages each z plane of a field (a 2D box with a halo) into
+// shared memory with one cp.async.bulk.tensor per array; an mbarrier per
+// pipeline stage counts the transaction bytes.  Boxes may start at negative
+// or out-of-range coordinates: the TMA unit fills those elements with zeros,
+// which is how grid edges are handled.  The innermost coordinate of every
+// load is a multiple of 16 bytes (callers round x down), and every wait is
+// bounded: after kMbarSpinLimit polls it gives up and reports failure.
+#pragma once
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+
+constexpr unsigned kMbarSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Make barrier initialisation visible to the async (TMA) proxy; follow
+// with __syncthreads before any thread waits or any copy is issued.
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the phase with the given parity to complete; false once
+// kMbarSpinLimit polls or kMbarWaitNs nanoseconds have passed.
+constexpr uint64_t kMbarWaitNs = 500000000ull;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (unsigned k = 0; k < kMbarSpinLimit; ++k) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((k & 255) == 255 && global_ns() - t0 > kMbarWaitNs) return false;
+    }
+    return false;
+}
+
+// 3D tiled load of the box at (x, y, z) into shared memory, completing on bar.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_map(const CUtensorMap* map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
+}
+
+// Host: encode a 3D tiled map over a dense (d, h, w) array of elem-byte
+// elements with box (bx, by, 1); false when the driver rejects it (base,
+// stride or box alignment) -- callers then use their non-TMA path.
+bool encode_map_3d(CUtensorMap* map, const void* base, int elem, i64 w, i64 h, i64 d, int bx, int by);
+
+}  // namespace pg
