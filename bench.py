@@ -416,7 +416,9 @@ def ours(args, spec, dims):
     its = [s["iterations"] for s in stats]
     # Kernel breakdown: the same number of further steps with a CUDA-event
     # pair around every launch (stream-launched loops, so each kernel is
-    # timed on the stream it runs on).
+    # timed on the stream it runs on).  The host-polled CG loop of this mode
+    # launches iterations past its stop test, which exit at entry: per-kind
+    # figures count only the launches that did work.
     import ctypes as C
 
     lib.pg_profile_reset()
@@ -427,7 +429,7 @@ def ours(args, spec, dims):
     for k in range(lib.pg_profile_num_kinds()):
         t = C.c_double()
         n = C.c_int64()
-        lib.pg_profile_read(k, C.byref(t), C.byref(n))
+        lib.pg_profile_read_active(k, C.byref(t), C.byref(n))
         if n.value:
             kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
     # --- plain FP32 PCG on the same workload -------------------------------
@@ -650,7 +652,7 @@ def bench_learned(args):
     kinds = {}
     for k in range(lib.pg_profile_num_kinds()):
         t, n = C.c_double(), C.c_int64()
-        lib.pg_profile_read(k, C.byref(t), C.byref(n))
+        lib.pg_profile_read_active(k, C.byref(t), C.byref(n))
         if n.value:
             kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
     peak, src = bf16_peak()
@@ -760,7 +762,7 @@ def bench_batch(args):
     kinds = {}
     for k in range(lib.pg_profile_num_kinds()):
         t, n = C.c_double(), C.c_int64()
-        lib.pg_profile_read(k, C.byref(t), C.byref(n))
+        lib.pg_profile_read_active(k, C.byref(t), C.byref(n))
         if n.value:
             kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
     # comparison: batched Jacobi-PCG on the same state (one step)

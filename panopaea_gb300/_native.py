@@ -155,6 +155,7 @@ _SIGS = {
     "pg_profile_num_kinds": (_I, []),
     "pg_profile_kind_name": (C.c_char_p, [_I]),
     "pg_profile_read": (_I, [_I, C.POINTER(_D), C.POINTER(_I64)]),
+    "pg_profile_read_active": (_I, [_I, C.POINTER(_D), C.POINTER(_I64)]),
 }
 for _sfx in ("f32", "f64"):
     _SIGS.update({

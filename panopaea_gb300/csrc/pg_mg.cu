@@ -63,7 +63,8 @@ struct MgHierarchy {
     // between z and e0b; tensor maps of the flags and of the vectors met
     bool pairs = false;
     float* e0b = nullptr;
-    CUtensorMap gmap;
+    CUtensorMap gmap;  // level-0 flags
+    CUtensorMap cmap;  // level-1 correction (prolongation)
     int pair_cap = 0;  // resident k_mg_pair blocks on the device
     struct MapEnt {
         const void* p = nullptr;
@@ -230,73 +231,93 @@ constexpr int kPGw = kPX + 32, kPGh = kPY + 2;   // flags box from (x0 - 16, y0 
 constexpr int kPEBytes = kPEw * kPEh * 4;        // 3456
 constexpr int kPFBytes = kPFw * kPFh * 4;        // 2880
 constexpr int kPGBytes = kPGw * kPGh;            // 960
+constexpr int kPCw = kPX / 2 + 8, kPCh = kPY / 2 + 2;  // coarse-correction box from (x0/2 - 4, y0/2 - 1)
+constexpr int kPCBytes = kPCw * kPCh * 4;        // 960
 constexpr int kPFOff = kPEBytes;                 // every box starts on 128 bytes
 constexpr int kPGOff = kPFOff + ((kPFBytes + 127) / 128) * 128;
-constexpr int kPStageBytes = kPGOff + ((kPGBytes + 127) / 128) * 128;
+constexpr int kPCOff = kPGOff + ((kPGBytes + 127) / 128) * 128;
 constexpr int kPSw = kPX + 2, kPSh = kPY + 2;    // new c1 values of one plane (tile + ring)
 constexpr int kPSlotBytes = kPSw * kPSh * 4;
-constexpr int kPBarOff = kPStages * kPStageBytes + 4 * kPSlotBytes;
-constexpr size_t kPSmem = 128 + kPBarOff + kPStages * 8;
-static_assert(kPEBytes % 128 == 0 && kPStageBytes % 128 == 0, "TMA boxes must stay 128-byte aligned");
 
 enum { PR_SELF = 0 /* c1 = f * invd (e = 0 before) */, PR_PLAIN = 1, PR_PROLONG = 2 /* ein + ec[parent] */ };
+
+// Shared-memory layout per first-sweep mode: the prolonging pair also
+// stages the coarse correction's parent plane and runs one stage fewer
+// (four blocks stay resident per SM).
+template <int M1> struct PairCfg {
+    static constexpr bool kCoarse = M1 == PR_PROLONG;
+    static constexpr int kStages = kCoarse ? 5 : kPStages;
+    static constexpr int kStageBytes = kPCOff + (kCoarse ? ((kPCBytes + 127) / 128) * 128 : 0);
+    static constexpr int kBarOff = kStages * kStageBytes + 4 * kPSlotBytes;
+    static constexpr size_t kSmem = 128 + kBarOff + kStages * 8;
+    static constexpr unsigned kTx = (M1 == PR_SELF ? 0 : kPEBytes) + kPFBytes + kPGBytes + (kCoarse ? kPCBytes : 0);
+    static_assert(kStageBytes % 128 == 0 && kPEBytes % 128 == 0, "TMA boxes must stay 128-byte aligned");
+};
 
 struct PairArgs {
     int d, h, w;
     float dt;
     float* eout;
-    const float* ec;  // PR_PROLONG: correction of the next coarser level
-    int cw, ch;
-    int c1;           // colour of the first half-sweep
+    int c1;  // colour of the first half-sweep
     int tiles_x, tiles_y, zc, nwork;
 };
 
 template <int M1, bool RZ>
-__global__ void __launch_bounds__(kPThreads)
+__global__ void __launch_bounds__(kPThreads, 4)
     k_mg_pair(const __grid_constant__ CUtensorMap emap, const __grid_constant__ CUtensorMap fmap,
-              const __grid_constant__ CUtensorMap gmap, PairArgs a, CgState* st, double* partials) {
+              const __grid_constant__ CUtensorMap gmap, const __grid_constant__ CUtensorMap cmap, PairArgs a,
+              CgState* st, double* partials) {
+    typedef PairCfg<M1> Cfg;
+    constexpr int kStages = Cfg::kStages, kStageBytes = Cfg::kStageBytes;
     if (st->done) return;
     extern __shared__ unsigned char pair_smem_raw[];
     __shared__ double sm[32];
     __shared__ float inv_tab[8];  // 1 / (n dt) for n open faces (0 for n = 0), as Cell<true>
-    unsigned char* const base = (unsigned char*)(((uintptr_t)pair_smem_raw + 127) & ~(uintptr_t)127);
-    float(*const S1)[kPSh][kPSw] = (float(*)[kPSh][kPSw])(base + kPStages * kPStageBytes);
-    uint64_t* const bars = (uint64_t*)(base + kPBarOff);
+    // 128-byte aligned by an offset (pointer arithmetic keeps every access
+    // below in the shared window: LDS/STS, not generic loads)
+    unsigned char* const base = pair_smem_raw + ((128u - (smem_u32(pair_smem_raw) & 127u)) & 127u);
+    float(*const S1)[kPSh][kPSw] = (float(*)[kPSh][kPSw])(base + kStages * kStageBytes);
+    uint64_t* const bars = (uint64_t*)(base + Cfg::kBarOff);
     const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
     const float dt = a.dt;
     if (tid == 0) {
-        for (int s = 0; s < kPStages; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
         mbar_fence_init();
         if (M1 != PR_SELF) tma_prefetch_map(&emap);
+        if (Cfg::kCoarse) tma_prefetch_map(&cmap);
         tma_prefetch_map(&fmap);
         tma_prefetch_map(&gmap);
     }
     if (tid < 8) inv_tab[tid] = tid ? __frcp_rn((float)tid * dt) : 0.f;
     __syncthreads();
-    constexpr unsigned kTx = (M1 == PR_SELF ? 0 : kPEBytes) + kPFBytes + kPGBytes;
     const int h = a.h, w = a.w, d = a.d;
     const int per_plane = a.tiles_x * a.tiles_y;
-    auto stage = [&](unsigned j) -> const unsigned char* { return base + (j % kPStages) * kPStageBytes; };
+    auto stage = [&](unsigned j) -> const unsigned char* { return base + (j % kStages) * kStageBytes; };
     auto Ev = [](const unsigned char* P, int r, int c) -> float { return ((const float*)P)[r * kPEw + c]; };
     auto Fv = [](const unsigned char* P, int r, int c) -> float {
         return ((const float*)(P + kPFOff))[r * kPFw + c];
     };
     auto Gv = [](const unsigned char* P, int r, int c) -> unsigned { return (P + kPGOff)[r * kPGw + c]; };
+    // coarse correction at the parent of tile cell (yl, xl) of the staged plane
+    auto Cv = [](const unsigned char* P, int yl, int xl) -> float {
+        return ((const float*)(P + kPCOff))[((yl >> 1) + 1) * kPCw + (xl >> 1) + 4];
+    };
     unsigned issued_end = 0;  // thread 0: one past the last plane issued
     auto issue = [&](unsigned j, int plane, int x0, int y0) {
         issued_end = j + 1;
-        unsigned char* dst = base + (j % kPStages) * kPStageBytes;
-        uint64_t* bar = &bars[j % kPStages];
-        mbar_expect_tx(bar, kTx);
+        unsigned char* dst = base + (j % kStages) * kStageBytes;
+        uint64_t* bar = &bars[j % kStages];
+        mbar_expect_tx(bar, Cfg::kTx);
         if (M1 != PR_SELF) tma_load_3d(dst, &emap, bar, x0 - 4, y0 - 2, plane);
         tma_load_3d(dst + kPFOff, &fmap, bar, x0 - 4, y0 - 1, plane);
         tma_load_3d(dst + kPGOff, &gmap, bar, x0 - 16, y0 - 1, plane);
+        if (Cfg::kCoarse) tma_load_3d(dst + kPCOff, &cmap, bar, x0 / 2 - 4, y0 / 2 - 1, plane >> 1);
     };
     // Thread 0 alone polls the barriers; the __syncthreads that follows its
     // wait publishes the staged plane to the block.
     bool ok = true;
     auto wait = [&](unsigned j) {
-        if (tid == 0 && ok) ok = mbar_wait(&bars[j % kPStages], (j / kPStages) & 1);
+        if (tid == 0 && ok) ok = mbar_wait(&bars[j % kStages], (j / kStages) & 1);
     };
     // Gauss-Seidel update from the open-face neighbour values (same
     // operation order as k_mg_smooth<true, ...>; the loads are unconditional,
@@ -320,7 +341,7 @@ __global__ void __launch_bounds__(kPThreads)
         const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
         const int n = z1 - z0 + 4;  // planes z0 - 2 .. z1 + 1 (ring index j = plane - z0 + 2)
         if (tid == 0)
-            for (int j = 0; j < min(n, kPStages); ++j) issue(seq + j, z0 - 2 + j, x0, y0);
+            for (int j = 0; j < min(n, kStages); ++j) issue(seq + j, z0 - 2 + j, x0, y0);
         wait(seq);
         wait(seq + 1);
         wait(seq + 2);
@@ -336,20 +357,11 @@ __global__ void __launch_bounds__(kPThreads)
                 const unsigned fl = Gv(P0, yl + 1, xl + 16);
                 const float fv = Fv(P0, yl + 1, xl + 4);
                 if (M1 == PR_SELF) return fv * inv_tab[__popc(fl)];
-                if (M1 == PR_PROLONG) {  // the coarse correction only behind open faces
-                    const int gy = y0 + yl, gx = x0 + xl;
-                    auto nb = [&](float v, int z, int y, int x) -> float {
-                        return v + a.ec[((z >> 1) * a.ch + (y >> 1)) * a.cw + (x >> 1)];
-                    };
-                    float s = fv;
-                    if (fl & XLO) s += dt * nb(Ev(P0, yl + 2, xl + 3), p, gy, gx - 1);
-                    if (fl & XHI) s += dt * nb(Ev(P0, yl + 2, xl + 5), p, gy, gx + 1);
-                    if (fl & YLO) s += dt * nb(Ev(P0, yl + 1, xl + 4), p, gy - 1, gx);
-                    if (fl & YHI) s += dt * nb(Ev(P0, yl + 3, xl + 4), p, gy + 1, gx);
-                    if (fl & ZLO) s += dt * nb(Ev(Pm, yl + 2, xl + 4), p - 1, gy, gx);
-                    if (fl & ZHI) s += dt * nb(Ev(Pp, yl + 2, xl + 4), p + 1, gy, gx);
-                    return s * inv_tab[__popc(fl)];
-                }
+                if (M1 == PR_PROLONG)  // neighbours plus their parents' coarse correction
+                    return gs(fl, fv, Ev(P0, yl + 2, xl + 3) + Cv(P0, yl, xl - 1),
+                              Ev(P0, yl + 2, xl + 5) + Cv(P0, yl, xl + 1), Ev(P0, yl + 1, xl + 4) + Cv(P0, yl - 1, xl),
+                              Ev(P0, yl + 3, xl + 4) + Cv(P0, yl + 1, xl), Ev(Pm, yl + 2, xl + 4) + Cv(Pm, yl, xl),
+                              Ev(Pp, yl + 2, xl + 4) + Cv(Pp, yl, xl));
                 return gs(fl, fv, Ev(P0, yl + 2, xl + 3), Ev(P0, yl + 2, xl + 5), Ev(P0, yl + 1, xl + 4),
                           Ev(P0, yl + 3, xl + 4), Ev(Pm, yl + 2, xl + 4), Ev(Pp, yl + 2, xl + 4));
             };
@@ -373,7 +385,7 @@ __global__ void __launch_bounds__(kPThreads)
                 break;
             }
             // the ring slot of plane p - 2 is free now: load kPStages planes past it
-            if (tid == 0 && i >= 1 && i - 1 + kPStages < n) issue(seq + i - 1 + kPStages, z0 - 3 + i + kPStages, x0, y0);
+            if (tid == 0 && i >= 1 && i - 1 + kStages < n) issue(seq + i - 1 + kStages, z0 - 3 + i + kStages, x0, y0);
             if (i >= 2) {  // second half-sweep on plane q = p - 1, then store it
                 const int q = p - 1;
                 const int gy = y0 + ty;
@@ -401,8 +413,8 @@ __global__ void __launch_bounds__(kPThreads)
     if (failed) {  // a plane never arrived: drain the copies in flight (bounded), stop the solve
         if (tid == 0) {
             const uint64_t t0 = global_ns();
-            for (unsigned j = issued_end > kPStages ? issued_end - kPStages : 0; j < issued_end; ++j)
-                while (!mbar_try_wait(&bars[j % kPStages], (j / kPStages) & 1) && global_ns() - t0 < kMbarWaitNs) {
+            for (unsigned j = issued_end > kStages ? issued_end - kStages : 0; j < issued_end; ++j)
+                while (!mbar_try_wait(&bars[j % kStages], (j / kStages) & 1) && global_ns() - t0 < kMbarWaitNs) {
                 }
             st->status = PG_TIMEOUT;
             st->done = 1;
@@ -847,7 +859,8 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
 
 template <int M1, bool RZ>
 static int pair_attr() {
-    return (int)cudaFuncSetAttribute(k_mg_pair<M1, RZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
+    return (int)cudaFuncSetAttribute(k_mg_pair<M1, RZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)PairCfg<M1>::kSmem);
 }
 
 // Opt every instantiation into its shared memory and size the grid by the
@@ -856,9 +869,14 @@ static int pair_setup(pg_grid* g, MgHierarchy* H) {
     int e = pair_attr<PR_SELF, false>() | pair_attr<PR_PLAIN, false>() | pair_attr<PR_PROLONG, false>() |
             pair_attr<PR_PLAIN, true>() | pair_attr<PR_PROLONG, true>();
     if (e) return cuda_fail((cudaError_t)e, "cudaFuncSetAttribute(k_mg_pair)");
-    int bps = 0;
-    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_mg_pair<PR_PLAIN, false>, kPThreads, kPSmem));
-    H->pair_cap = std::min(bps * g->num_sms, kMaxBlocks);
+    int bps = 0, bps2 = 0;
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_mg_pair<PR_PLAIN, false>, kPThreads,
+                                                          PairCfg<PR_PLAIN>::kSmem));
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps2, k_mg_pair<PR_PROLONG, false>, kPThreads,
+                                                          PairCfg<PR_PROLONG>::kSmem));
+    H->pair_cap = std::min(std::min(bps, bps2) * g->num_sms, kMaxBlocks);
+    const MgLevel& C = H->lv[1];
+    if (!encode_map_3d(&H->cmap, C.e, 4, C.D.w, C.D.h, C.D.d, kPCw, kPCh)) H->pair_cap = 0;
     return PG_OK;
 }
 
@@ -901,10 +919,6 @@ static bool pair_plan(const MgHierarchy& H, const float* r, const float* z, Pair
     a.zc = (a.d + nch - 1) / nch;
     a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
     P->nb = std::max(1, std::min(a.nwork, H.pair_cap));
-    if (H.nlev > 1) {
-        a.cw = (int)H.lv[1].D.w;
-        a.ch = (int)H.lv[1].D.h;
-    }
     return true;
 }
 
@@ -912,16 +926,17 @@ template <int M1, bool RZ>
 static void pair_t(pg_grid* g, const MgHierarchy& H, const CUtensorMap* em, const PairLaunch& P, const PairArgs& a) {
     cudaStream_t s = g->stream;
     PG_LAUNCH(KK_MG_PAIR, s,
-              k_mg_pair<M1, RZ><<<P.nb, kPThreads, kPSmem, s>>>(*em, *P.fm, H.gmap, a, g->ws.state, g->ws.partials));
+              k_mg_pair<M1, RZ><<<P.nb, kPThreads, PairCfg<M1>::kSmem, s>>>(*em, *P.fm, H.gmap, H.cmap, a,
+                                                                            g->ws.state, g->ws.partials));
 }
 
 // One fused pair: first half-sweep over colour c1 in `mode` from ein
-// (unused for PR_SELF), second over the other colour; both into eout.
+// (unused for PR_SELF; PR_PROLONG adds the level-1 correction), second
+// over the other colour; both into eout.
 static void pair(pg_grid* g, const MgHierarchy& H, const PairLaunch& P, int mode, int c1, bool rz, const float* ein,
-                 float* eout, const float* ec) {
+                 float* eout) {
     PairArgs a = P.a;
     a.eout = eout;
-    a.ec = ec;
     a.c1 = c1;
     const CUtensorMap* em = vec_map(H, ein ? ein : H.e0b, kPEh);  // cached by pair_plan
     if (mode == PR_SELF) pair_t<PR_SELF, false>(g, H, em, P, a);
@@ -1010,8 +1025,8 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
         float* e = E(l);
         const float* f = F(l);
         if (l == 0 && pairs) {
-            pair(g, H, P, PR_SELF, 0, false, nullptr, pout[0], nullptr);
-            for (int k = 1; k < nsmooth; ++k) pair(g, H, P, PR_PLAIN, 0, false, pout[(k - 1) & 1], pout[k & 1], nullptr);
+            pair(g, H, P, PR_SELF, 0, false, nullptr, pout[0]);
+            for (int k = 1; k < nsmooth; ++k) pair(g, H, P, PR_PLAIN, 0, false, pout[(k - 1) & 1], pout[k & 1]);
             e = pout[(nsmooth - 1) & 1];
         } else {
             // pre-smoothing: (red, black) x nsmooth from e = 0; the first red is implicit
@@ -1069,7 +1084,7 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
         if (l == 0 && pairs) {
             for (int k = nsmooth; k < 2 * nsmooth; ++k)
                 pair(g, H, P, k == nsmooth ? PR_PROLONG : PR_PLAIN, 1, k == 2 * nsmooth - 1, pout[(k - 1) & 1],
-                     pout[k & 1], k == nsmooth ? ec : nullptr);
+                     pout[k & 1]);
             continue;
         }
         // post-smoothing: (black, red) x nsmooth; the first black reads the

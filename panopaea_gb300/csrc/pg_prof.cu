@@ -1,4 +1,5 @@
 // pg_prof.cu -- launch counting and per-kernel CUDA-event timing.
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 #include <deque>
@@ -33,6 +34,7 @@ struct Prof {
     cudaEvent_t open[KK_COUNT] = {};
     double ms[KK_COUNT] = {};
     int64_t n[KK_COUNT] = {};
+    std::vector<float> each[KK_COUNT];  // every launch's duration
 };
 
 Prof& prof() {
@@ -64,6 +66,7 @@ void drain(Prof& p, bool wait) {
         if (cudaEventElapsedTime(&ms, q.a, q.b) == cudaSuccess) {
             p.ms[q.kind] += ms;
             p.n[q.kind] += 1;
+            p.each[q.kind].push_back(ms);
         }
         p.pool.push_back(q.a);
         p.pool.push_back(q.b);
@@ -140,6 +143,7 @@ int pg_profile_reset(void) {
     for (int k = 0; k < KK_COUNT; ++k) {
         p.ms[k] = 0.0;
         p.n[k] = 0;
+        p.each[k].clear();
     }
     return PG_OK;
 }
@@ -158,6 +162,25 @@ int pg_profile_read(int kind, double* total_ms, int64_t* launches) {
     drain(p, true);
     if (total_ms) *total_ms = p.ms[kind];
     if (launches) *launches = p.n[kind];
+    return PG_OK;
+}
+
+int pg_profile_read_active(int kind, double* total_ms, int64_t* launches) {
+    if (kind < 0 || kind >= KK_COUNT) return bad_arg("pg_profile_read_active: unknown kind");
+    Prof& p = prof();
+    std::lock_guard<std::mutex> lk(p.m);
+    drain(p, true);
+    float mx = 0.f;
+    for (float v : p.each[kind]) mx = std::max(mx, v);
+    double t = 0.0;
+    int64_t n = 0;
+    for (float v : p.each[kind])
+        if (v >= 0.25f * mx) {
+            t += v;
+            ++n;
+        }
+    if (total_ms) *total_ms = t;
+    if (launches) *launches = n;
     return PG_OK;
 }
 

@@ -105,6 +105,30 @@ def test_profile_counters(pg):
     n = C.c_int64()
     lib.pg_profile_read(names.index("dec_op"), C.byref(t), C.byref(n))
     assert n.value >= 1 and t.value > 0
+    ta, na = C.c_double(), C.c_int64()
+    lib.pg_profile_read_active(names.index("dec_op"), C.byref(ta), C.byref(na))
+    assert 1 <= na.value <= n.value and 0 < ta.value <= t.value
+
+
+def test_profile_active_skips_exit_at_entry_launches(pg, oracle):
+    """The host-polled CG loop (profiling mode) launches iterations past its
+    stop test; they exit at entry, and the active count leaves them out."""
+    import ctypes as C
+
+    lib = pg.load()
+    names = [lib.pg_profile_kind_name(k).decode() for k in range(lib.pg_profile_num_kinds())]
+    lib.pg_profile_reset()
+    lib.pg_profile_enable(1)
+    try:
+        st, *_ = solve_case(pg, oracle, (192, 192, 192), False, 2, 1e-5)  # real launches >> exit-at-entry ones
+    finally:
+        lib.pg_profile_enable(0)
+    k = names.index("cg_spmv")
+    t, n, ta, na = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
+    lib.pg_profile_read(k, C.byref(t), C.byref(n))
+    lib.pg_profile_read_active(k, C.byref(ta), C.byref(na))
+    assert st["status"] == 0
+    assert na.value == st["iterations"] <= n.value, (na.value, n.value, st["iterations"])
 
 
 @pytest.mark.parametrize("precond", [0, 1, 2])
