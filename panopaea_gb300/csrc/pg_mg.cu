@@ -595,60 +595,70 @@ __device__ __forceinline__ void tail_restrict(const LV& v, const float* e, const
 constexpr int kTailThreads = 1024;
 constexpr int kTailSmemMax = 220 * 1024;
 
-__global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs A, CgState* st) {
-    if (st->done) return;
-    extern __shared__ float tsm[];
-    LV v[kMaxLevels];
-    float* E[kMaxLevels];
-    float* F[kMaxLevels];
-    // carve the shared memory: wx, wy, wz, invd, e, f per level
-    float* p = tsm;
+// Levels [A.lt, A.nl) by the calling block in its shared memory tsm.
+__device__ __forceinline__ void tail_body(const TailArgs& A, float* tsm) {
+    // Shared memory per level: wx, wy, wz, invd, e, f (n floats each).  The
+    // level views are rebuilt from tsm + offset at every use, so every
+    // access stays a shared-window access (a table of pointers would make
+    // them generic loads).
+    auto ncell = [&](int l) { return A.L[l].d * A.L[l].h * A.L[l].w; };
+    auto off = [&](int l) {
+        int o = 0;
+        for (int k = A.lt; k < l; ++k) o += 6 * ncell(k);
+        return o;
+    };
+    auto lv = [&](int l) -> LV {
+        const TailLevel& T = A.L[l];
+        const int n = ncell(l);
+        float* p = tsm + off(l);
+        LV v;
+        v.nd = T.nd;
+        v.d = T.d;
+        v.h = T.h;
+        v.w = T.w;
+        v.flags = nullptr;
+        v.wx = p;
+        v.wy = p + n;
+        v.wz = p + 2 * n;
+        v.invd = p + 3 * n;
+        v.dt = 0.f;
+        return v;
+    };
+    auto E = [&](int l) -> float* { return tsm + off(l) + 4 * ncell(l); };
+    auto F = [&](int l) -> float* { return tsm + off(l) + 5 * ncell(l); };
     for (int l = A.lt; l < A.nl; ++l) {
         const TailLevel& T = A.L[l];
-        const int n = T.d * T.h * T.w;
-        float* wx = p;
-        float* wy = p + n;
-        float* wz = p + 2 * n;
-        float* iv = p + 3 * n;
-        E[l] = p + 4 * n;
-        F[l] = p + 5 * n;
-        p += 6 * n;
+        const int n = ncell(l);
+        float* p = tsm + off(l);
         for (int c = threadIdx.x; c < n; c += blockDim.x) {
-            wx[c] = T.wx[c];
-            wy[c] = T.wy[c];
-            wz[c] = T.nd == 3 ? T.wz[c] : 0.f;
-            iv[c] = T.invd[c];
-            if (l == A.lt) F[l][c] = A.f_in[c];
+            p[c] = T.wx[c];
+            p[n + c] = T.wy[c];
+            p[2 * n + c] = T.nd == 3 ? T.wz[c] : 0.f;
+            p[3 * n + c] = T.invd[c];
+            if (l == A.lt) p[5 * n + c] = A.f_in[c];
         }
-        v[l].nd = T.nd;
-        v[l].d = T.d;
-        v[l].h = T.h;
-        v[l].w = T.w;
-        v[l].flags = nullptr;
-        v[l].wx = wx;
-        v[l].wy = wy;
-        v[l].wz = wz;
-        v[l].invd = iv;
-        v[l].dt = 0.f;
     }
     __syncthreads();
     const int nl = A.nl, ns = A.nsmooth;
     // down
     for (int l = A.lt; l + 1 < nl; ++l) {
-        const LV& c = v[l + 1];
-        tail_smooth<NB_FIRST>(v[l], E[l], F[l], nullptr, c.w, c.h, 1);
-        if (ns == 1) tail_smooth<NB_SELF>(v[l], E[l], F[l], nullptr, c.w, c.h, 0);
+        const TailLevel& c = A.L[l + 1];
+        const LV v = lv(l);
+        float* e = E(l);
+        const float* f = F(l);
+        tail_smooth<NB_FIRST>(v, e, f, nullptr, c.w, c.h, 1);
+        if (ns == 1) tail_smooth<NB_SELF>(v, e, f, nullptr, c.w, c.h, 0);
         for (int k = 1; k < ns; ++k) {
-            tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 0);
-            tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 1);
+            tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 0);
+            tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 1);
         }
-        tail_restrict(v[l], E[l], F[l], F[l + 1], c.d, c.h, c.w);
+        tail_restrict(v, e, f, F(l + 1), c.d, c.h, c.w);
     }
     // coarsest: symmetric red-black Gauss-Seidel from e = 0
     {
-        const LV& cv = v[nl - 1];
-        float* e = E[nl - 1];
-        const float* f = F[nl - 1];
+        const LV cv = lv(nl - 1);
+        float* e = E(nl - 1);
+        const float* f = F(nl - 1);
         const int n = cv.d * cv.h * cv.w;
         for (int c = threadIdx.x; c < n; c += blockDim.x) e[c] = 0.f;
         __syncthreads();
@@ -660,15 +670,25 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs A, CgState* s
     }
     // up
     for (int l = nl - 2; l >= A.lt; --l) {
-        const LV& c = v[l + 1];
-        tail_smooth<NB_PROLONG>(v[l], E[l], F[l], E[l + 1], c.w, c.h, 1);
+        const TailLevel& c = A.L[l + 1];
+        const LV v = lv(l);
+        float* e = E(l);
+        const float* f = F(l);
+        tail_smooth<NB_PROLONG>(v, e, f, E(l + 1), c.w, c.h, 1);
         for (int k = 0; k < ns; ++k) {
-            if (k > 0) tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 1);
-            tail_smooth<NB_PLAIN>(v[l], E[l], F[l], nullptr, c.w, c.h, 0);
+            if (k > 0) tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 1);
+            tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 0);
         }
     }
-    const int n0 = A.L[A.lt].d * A.L[A.lt].h * A.L[A.lt].w;
-    for (int c = threadIdx.x; c < n0; c += blockDim.x) A.e_out[c] = E[A.lt][c];
+    const int n0 = ncell(A.lt);
+    const float* e0 = E(A.lt);
+    for (int c = threadIdx.x; c < n0; c += blockDim.x) A.e_out[c] = e0[c];
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs A, CgState* st) {
+    if (st->done) return;
+    extern __shared__ float tsm[];
+    tail_body(A, tsm);
 }
 
 // Coarse face weights: half the sum of the fine weights on the coarse face.
@@ -946,6 +966,43 @@ static void pair(pg_grid* g, const MgHierarchy& H, const PairLaunch& P, int mode
     else pair_t<PR_PLAIN, false>(g, H, em, P, a);
 }
 
+// ---------------------------------------------------------------------------
+// Tail launch.
+
+static size_t tail_smem(const MgHierarchy& H) {
+    size_t smem = 0;
+    for (int l = H.tail; l < H.nlev; ++l) smem += 6 * sizeof(float) * (size_t)H.lv[l].D.nc();
+    return smem;
+}
+
+static TailArgs tail_args(const MgHierarchy& H, int nsmooth) {
+    TailArgs A;
+    A.lt = H.tail;
+    A.nl = H.nlev;
+    A.nsmooth = nsmooth;
+    A.e_out = H.lv[H.tail].e;
+    A.f_in = H.lv[H.tail].f;
+    for (int l = H.tail; l < H.nlev; ++l) {
+        const MgLevel& L = H.lv[l];
+        A.L[l] = TailLevel{L.D.nd, (int)L.D.d, (int)L.D.h, (int)L.D.w, L.wx, L.wy, L.wz, L.invd};
+    }
+    return A;
+}
+
+// The single-block tail: levels [H.tail, nl).
+static int launch_tail(pg_grid* g, const MgHierarchy& H, int nsmooth) {
+    const TailArgs A = tail_args(H, nsmooth);
+    const size_t smem = tail_smem(H);
+    static bool attr = false;
+    if (!attr) {
+        PG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax));
+        attr = true;
+    }
+    if (smem > (size_t)kTailSmemMax) return bad_arg("PG_PRECOND_MG: multigrid tail does not fit in shared memory");
+    PG_LAUNCH(KK_MG_COARSE, g->stream, k_mg_tail<<<1, kTailThreads, smem, g->stream>>>(A, g->ws.state));
+    return PG_OK;
+}
+
 // Launch one half-sweep over `color` at level l.
 template <bool L0, int MODE, bool RZ>
 static void smooth(pg_grid* g, const MgHierarchy& H, int l, float* e, const float* f, const float* ec, int color) {
@@ -1052,25 +1109,8 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
                                                                                   g->ws.state));
     }
     if (tail) {
-        TailArgs A;
-        A.lt = top;
-        A.nl = nl;
-        A.nsmooth = nsmooth;
-        A.e_out = H.lv[top].e;
-        A.f_in = H.lv[top].f;
-        size_t smem = 0;
-        for (int l = top; l < nl; ++l) {
-            const MgLevel& L = H.lv[l];
-            A.L[l] = TailLevel{L.D.nd, (int)L.D.d, (int)L.D.h, (int)L.D.w, L.wx, L.wy, L.wz, L.invd};
-            smem += 6 * sizeof(float) * (size_t)L.D.nc();
-        }
-        static bool attr = false;
-        if (!attr) {
-            PG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax));
-            attr = true;
-        }
-        if (smem > (size_t)kTailSmemMax) return bad_arg("PG_PRECOND_MG: multigrid tail does not fit in shared memory");
-        PG_LAUNCH(KK_MG_COARSE, s, k_mg_tail<<<1, kTailThreads, smem, s>>>(A, g->ws.state));
+        const int rc = launch_tail(g, H, nsmooth);
+        if (rc) return rc;
     } else {
         const LV v = view(H, nl - 1);
         PG_LAUNCH(KK_MG_COARSE, s,
