@@ -222,9 +222,12 @@ __global__ void __launch_bounds__(kMgThreads)
 // per thread.  Per cell: 4 bytes of ein, 4 of f and 1 of flags read, 4 of
 // eout written -- half the traffic of two separate half-sweeps.  The
 // arithmetic of every cell is that of k_mg_smooth<true, ...>.
-constexpr int kPX = 64, kPY = 8;
-constexpr int kPThreads = 256;  // one (c1, c2) x-pair per thread and plane
-constexpr int kPStages = 6;     // plane ring; loads run kPStages - 3 planes ahead
+constexpr int kPX = 64;
+constexpr int kPWarps = 8, kPRows = 2;  // warps per block, tile rows per thread
+constexpr int kPY = kPWarps * kPRows;
+constexpr int kPThreads = 32 * kPWarps;  // one (c1, c2) x-pair per thread, row and plane
+constexpr int kPMinBlocks = 2;           // resident blocks per SM the registers are sized for
+constexpr int kPStages = 6;              // plane ring; loads run kPStages - 3 planes ahead
 constexpr int kPEw = kPX + 8, kPEh = kPY + 4;    // ein box from (x0 - 4, y0 - 2)
 constexpr int kPFw = kPX + 8, kPFh = kPY + 2;    // f box from (x0 - 4, y0 - 1)
 constexpr int kPGw = kPX + 32, kPGh = kPY + 2;   // flags box from (x0 - 16, y0 - 1)
@@ -243,7 +246,7 @@ enum { PR_SELF = 0 /* c1 = f * invd (e = 0 before) */, PR_PLAIN = 1, PR_PROLONG 
 
 // Shared-memory layout per first-sweep mode: the prolonging pair also
 // stages the coarse correction's parent plane and runs one stage fewer
-// (four blocks stay resident per SM).
+// (kPMinBlocks blocks stay resident per SM).
 template <int M1> struct PairCfg {
     static constexpr bool kCoarse = M1 == PR_PROLONG;
     static constexpr int kStages = kCoarse ? 5 : kPStages;
@@ -263,7 +266,7 @@ struct PairArgs {
 };
 
 template <int M1, bool RZ>
-__global__ void __launch_bounds__(kPThreads, 4)
+__global__ void __launch_bounds__(kPThreads, kPMinBlocks)
     k_mg_pair(const __grid_constant__ CUtensorMap emap, const __grid_constant__ CUtensorMap fmap,
               const __grid_constant__ CUtensorMap gmap, const __grid_constant__ CUtensorMap cmap, PairArgs a,
               CgState* st, double* partials) {
@@ -365,17 +368,19 @@ __global__ void __launch_bounds__(kPThreads, 4)
                 return gs(fl, fv, Ev(P0, yl + 2, xl + 3), Ev(P0, yl + 2, xl + 5), Ev(P0, yl + 1, xl + 4),
                           Ev(P0, yl + 3, xl + 4), Ev(Pm, yl + 2, xl + 4), Ev(Pp, yl + 2, xl + 4));
             };
-            {
-                const int xl = 2 * lane + ((a.c1 + y0 + ty + p) & 1);
-                S1[p & 3][ty + 1][xl + 1] = c1_cell(ty, xl);
+#pragma unroll
+            for (int r = 0; r < kPRows; ++r) {
+                const int yl = ty + r * kPWarps;
+                const int xl = 2 * lane + ((a.c1 + y0 + yl + p) & 1);
+                S1[p & 3][yl + 1][xl + 1] = c1_cell(yl, xl);
             }
             if (tid < 64) {  // ring rows y0 - 1 and y0 + kPY
                 const int yl = tid < 32 ? -1 : kPY;
                 const int xl = 2 * lane + ((a.c1 + y0 + yl + p) & 1);
                 S1[p & 3][yl + 1][xl + 1] = c1_cell(yl, xl);
-            } else if (tid < 80) {  // ring columns x0 - 1 and x0 + kPX
+            } else if (tid < 64 + 2 * kPY) {  // ring columns x0 - 1 and x0 + kPX
                 const int k = tid - 64;
-                const int xl = k < 8 ? -1 : kPX, yl = k & 7;
+                const int xl = k < kPY ? -1 : kPX, yl = k < kPY ? k : k - kPY;
                 if (((x0 + xl + y0 + yl + p) & 1) == a.c1) S1[p & 3][yl + 1][xl + 1] = c1_cell(yl, xl);
             }
             // the next step's plane p + 2 must have landed
@@ -388,20 +393,24 @@ __global__ void __launch_bounds__(kPThreads, 4)
             if (tid == 0 && i >= 1 && i - 1 + kStages < n) issue(seq + i - 1 + kStages, z0 - 3 + i + kStages, x0, y0);
             if (i >= 2) {  // second half-sweep on plane q = p - 1, then store it
                 const int q = p - 1;
-                const int gy = y0 + ty;
-                const int xl2 = 2 * lane + ((a.c1 + 1 + gy + q) & 1), xl1 = xl2 ^ 1;
-                const float e1 = S1[q & 3][ty + 1][xl1 + 1];
-                const float fv = Fv(Pm, ty + 1, xl2 + 4);
-                const float e2 = gs(Gv(Pm, ty + 1, xl2 + 16), fv, S1[q & 3][ty + 1][xl2], S1[q & 3][ty + 1][xl2 + 2],
-                                    S1[q & 3][ty][xl2 + 1], S1[q & 3][ty + 2][xl2 + 1], S1[(q - 1) & 3][ty + 1][xl2 + 1],
-                                    S1[(q + 1) & 3][ty + 1][xl2 + 1]);
-                const int x = x0 + 2 * lane;
-                if (gy < h && x < w) {
-                    const float2 v = (xl1 & 1) ? make_float2(e2, e1) : make_float2(e1, e2);
-                    *(float2*)(a.eout + ((i64)q * h + gy) * w + x) = v;
-                    if (RZ) {
-                        acc.add(e1 * Fv(Pm, ty + 1, xl1 + 4));
-                        acc.add(e2 * fv);
+#pragma unroll
+                for (int r = 0; r < kPRows; ++r) {
+                    const int yl = ty + r * kPWarps, gy = y0 + yl;
+                    const int xl2 = 2 * lane + ((a.c1 + 1 + gy + q) & 1), xl1 = xl2 ^ 1;
+                    const float e1 = S1[q & 3][yl + 1][xl1 + 1];
+                    const float fv = Fv(Pm, yl + 1, xl2 + 4);
+                    const float e2 =
+                        gs(Gv(Pm, yl + 1, xl2 + 16), fv, S1[q & 3][yl + 1][xl2], S1[q & 3][yl + 1][xl2 + 2],
+                           S1[q & 3][yl][xl2 + 1], S1[q & 3][yl + 2][xl2 + 1], S1[(q - 1) & 3][yl + 1][xl2 + 1],
+                           S1[(q + 1) & 3][yl + 1][xl2 + 1]);
+                    const int x = x0 + 2 * lane;
+                    if (gy < h && x < w) {
+                        const float2 v = (xl1 & 1) ? make_float2(e2, e1) : make_float2(e1, e2);
+                        *(float2*)(a.eout + ((i64)q * h + gy) * w + x) = v;
+                        if (RZ) {
+                            acc.add(e1 * Fv(Pm, yl + 1, xl1 + 4));
+                            acc.add(e2 * fv);
+                        }
                     }
                 }
             }
