@@ -329,6 +329,67 @@ __global__ void __launch_bounds__(kCgThreads)
     }
 }
 
+// The update of the MG path (z.r comes from the V-cycle, so the only
+// reduction is the order-independent ||r||inf) on float4 vectors, two per
+// thread and iteration: eight cells' x, p, r, Ap in flight per thread.  Same
+// per-cell arithmetic as k_cg_update<float, PM_ZBUF>; n4 = n / 4.
+__global__ void __launch_bounds__(kCgThreads)
+    k_cg_update4(float4* __restrict__ x, float4* __restrict__ r, const float4* p0, const float4* p1,
+                 const float4* __restrict__ ap, i64 n4, CgState* st, double* partials) {
+    if (st->done) return;
+    __shared__ double sm[32];
+    const i64 k = *(volatile const i64*)&st->iter;
+    const float4* __restrict__ p = ((k + 1) & 1) ? p1 : p0;
+    const float alpha = (float)st->alpha, nalpha = -alpha;
+    float rm = 0.f;
+    int bad = 0;
+    auto one = [&](i64 c) {
+        const float4 xv = x[c], pv = p[c], rv = r[c], av = ap[c];
+        float4 xo, ro;
+        xo.x = xv.x + alpha * pv.x;
+        xo.y = xv.y + alpha * pv.y;
+        xo.z = xv.z + alpha * pv.z;
+        xo.w = xv.w + alpha * pv.w;
+        ro.x = rv.x + nalpha * av.x;
+        ro.y = rv.y + nalpha * av.y;
+        ro.z = rv.z + nalpha * av.z;
+        ro.w = rv.w + nalpha * av.w;
+        x[c] = xo;
+        r[c] = ro;
+        rm = fmaxf(fmaxf(fmaxf(rm, fabsf(ro.x)), fmaxf(fabsf(ro.y), fabsf(ro.z))), fabsf(ro.w));
+        bad |= !isfinite(ro.x) | !isfinite(ro.y) | !isfinite(ro.z) | !isfinite(ro.w);
+    };
+    const i64 stride = (i64)gridDim.x * blockDim.x;
+    i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; c + stride < n4; c += 2 * stride) {
+        one(c);
+        one(c + stride);
+    }
+    if (c < n4) one(c);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
+    const double m = block_max<kCgThreads>((double)rm, sm);
+    if (threadIdx.x == 0) partials[2 * kMaxBlocks + blockIdx.x] = m;
+    if (!last_block(&st->counter[2])) return;
+    const double rmax = reduce_partials<true, kCgThreads>(partials + 2 * kMaxBlocks, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+        st->counter[2] = 0;
+        const i64 it = st->iter + 1;
+        st->iter = it;
+        st->rmax = rmax;
+        if (st->nan_seen || !isfinite(rmax)) {
+            st->status = PG_NAN_DETECTED;
+            st->done = 1;
+        } else if ((float)rmax < (float)st->threshold) {  // pcg.rs:58-63
+            st->status = PG_OK;
+            st->done = 1;
+        } else if (it >= st->max_iter) {  // loop bound, pcg.rs:48
+            st->done = 1;
+        }
+    }
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
 // After max_iterations the reference has already run aux = M r and
 // search = aux + beta*search (pcg.rs:65-77); reproduce that tail.
 template <class T, int PM>
@@ -350,9 +411,17 @@ static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook
     PG_LAUNCH(KK_CG_SPMV, s,
               spmv_launch<T, PM>(s, g->num_sms, buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D, dt,
                                  g->ws.state, g->ws.partials, nb));
-    PG_LAUNCH(KK_CG_UPDATE, s,
-              k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, D.nc(),
-                                                           dt, g->ws.state, g->ws.partials));
+    const i64 n = D.nc();
+    if (PM == PM_ZBUF && sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.r) &&
+        aligned16(buf.p[0]) && aligned16(buf.p[1]) && aligned16(buf.ap))
+        PG_LAUNCH(KK_CG_UPDATE, s,
+                  k_cg_update4<<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.p[0],
+                                                         (const float4*)buf.p[1], (const float4*)buf.ap, n / 4,
+                                                         g->ws.state, g->ws.partials));
+    else
+        PG_LAUNCH(KK_CG_UPDATE, s,
+                  k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, n,
+                                                               dt, g->ws.state, g->ws.partials));
     if (PM == PM_ZBUF) hook->apply(g, buf.r, buf.z);
 }
 
