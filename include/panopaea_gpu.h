@@ -454,9 +454,10 @@ const char* pg_profile_kind_name(int kind);
 /* Waits for the recorded events and returns the summed device time (ms)
  * and launch count of one kernel kind. */
 int pg_profile_read(int kind, double* total_ms, int64_t* launches);
-/* The same over the launches that did work: those of at least a quarter of
- * the kind's longest launch (a CG loop polled from the host launches
- * iterations past its stop test, which exit at entry in microseconds). */
+/* The same over the launches that did work (a CG loop polled from the host
+ * launches iterations past its stop test, which exit at entry in a few
+ * microseconds): those of at least the smaller of a quarter of the kind's
+ * longest launch and the geometric mean of its shortest and longest. */
 int pg_profile_read_active(int kind, double* total_ms, int64_t* launches);
 
 #ifdef __cplusplus

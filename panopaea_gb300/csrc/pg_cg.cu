@@ -264,6 +264,10 @@ __global__ void __launch_bounds__(kTX * kTY)
 template <class T, int PM>
 static void spmv_launch(cudaStream_t s, int num_sms, const T* r, const T* zb, T* p0, T* p1, T* ap,
                         const uint8_t* flags, const Dims& D, T dt, CgState* st, double* partials, int nb_flat) {
+    if (PM == PM_ZBUF && sizeof(T) == 4 &&
+        spmv_tma_launch(s, num_sms, (const float*)zb, (float*)p0, (float*)p1, (float*)ap, flags, D, (float)dt, st,
+                        partials))
+        return;
     if (D.nd == 3) {
         const int tiles_x = (int)((D.w + kTX - 1) / kTX), tiles_y = (int)((D.h + kTY - 1) / kTY);
         const int cap = std::min(num_sms * 8, kMaxBlocks);

@@ -48,6 +48,12 @@ template <> struct Acc<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
+// The fused SpMV of the MG path on 3D float grids, TMA-staged (pg_spmv.cu);
+// false when it does not apply (2D, rows not a multiple of 16 cells, a
+// vector that cannot be mapped) and nothing was launched.
+bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, float* p1, float* ap,
+                     const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials);
+
 // Hooks for an outer preconditioner that produces z between the update
 // and the next SpMV (multigrid).  The last V-cycle kernel reduces z.r and
 // calls cg_finish_rz on the device state.

@@ -1,6 +1,7 @@
 // pg_prof.cu -- launch counting and per-kernel CUDA-event timing.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdlib>
 #include <deque>
 #include <mutex>
@@ -170,12 +171,19 @@ int pg_profile_read_active(int kind, double* total_ms, int64_t* launches) {
     Prof& p = prof();
     std::lock_guard<std::mutex> lk(p.m);
     drain(p, true);
-    float mx = 0.f;
-    for (float v : p.each[kind]) mx = std::max(mx, v);
+    // Exit-at-entry launches take a few microseconds, launches that did work
+    // are longer: split the two clusters at the smaller of a quarter of the
+    // longest launch and the geometric mean of the shortest and the longest.
+    float mx = 0.f, mn = 1e30f;
+    for (float v : p.each[kind]) {
+        mx = std::max(mx, v);
+        mn = std::min(mn, v);
+    }
+    const float cut = std::min(0.25f * mx, std::sqrt(mn * mx));
     double t = 0.0;
     int64_t n = 0;
     for (float v : p.each[kind])
-        if (v >= 0.25f * mx) {
+        if (v >= cut) {
             t += v;
             ++n;
         }

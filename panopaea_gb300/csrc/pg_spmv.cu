@@ -1,0 +1,294 @@
+// pg_spmv.cu -- the fused SpMV of the multigrid-preconditioned CG on 3D
+// grids, TMA-staged (p = z + beta p, Ap, p.Ap; pcg.rs:52-53, 77 with the
+// masked Laplacian of grid.rs).
+//
+// A block owns a kSX x kSY column tile and walks a chunk of z planes.  TMA
+// stages every plane of z and p_old (one-cell halo) and of the face flags
+// (tile only) into a kSStages-deep shared-memory ring; for plane q+1 the
+// block computes p_new = z + beta p_old on the tile and its one-cell ring
+// into a 4-slot plane ring (and stores the tile's values), then A p_new of
+// plane q from the slots of planes q-1, q and q+1.  A staged plane is free
+// as soon as its p_new and its flags have been used, so most of the ring is
+// in flight.  Per cell: 4 bytes of z, 4 of p_old, 1 of flags in; 4 of p_new
+// and 4 of Ap out.  Same per-cell arithmetic as k_cg_spmv3t<float, PM_ZBUF>
+// (the p.Ap reduction runs in a different order).
+#include <mutex>
+
+#include "pg_cg.cuh"
+#include "pg_tma.cuh"
+
+namespace pg {
+
+namespace {
+
+constexpr int kSX = 64, kSWarps = 8, kSRows = 2, kSY = kSWarps * kSRows;
+constexpr int kSThreads = 32 * kSWarps;
+constexpr int kSStages = 7;
+constexpr int kSVw = kSX + 8, kSVh = kSY + 2;  // z / p_old boxes from (x0 - 4, y0 - 1)
+constexpr int kSGw = kSX + 32, kSGh = kSY;     // flags box from (x0 - 16, y0)
+constexpr int kSVBytes = kSVw * kSVh * 4;
+constexpr int kSGBytes = kSGw * kSGh;
+constexpr int kSVPad = ((kSVBytes + 127) / 128) * 128;
+constexpr int kSPOff = kSVPad, kSGOff = 2 * kSVPad;
+constexpr int kSStageBytes = kSGOff + ((kSGBytes + 127) / 128) * 128;
+constexpr int kSSw = kSX + 2, kSSh = kSY + 2;  // p_new of one plane (tile + ring)
+constexpr int kSSlotBytes = kSSw * kSSh * 4;
+constexpr int kSBarOff = kSStages * kSStageBytes + 4 * kSSlotBytes;
+constexpr size_t kSSmem = 128 + kSBarOff + kSStages * 8;
+constexpr unsigned kSTx = 2 * kSVBytes + kSGBytes;
+static_assert(kSStageBytes % 128 == 0, "TMA boxes must stay 128-byte aligned");
+
+struct SpmvArgs {
+    int d, h, w;
+    float dt;
+    float* p0;
+    float* p1;
+    float* ap;
+    int tiles_x, tiles_y, zc, nwork;
+};
+
+__global__ void __launch_bounds__(kSThreads, 2)
+    k_cg_spmv3p(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap pmap0,
+                const __grid_constant__ CUtensorMap pmap1, const __grid_constant__ CUtensorMap gmap, SpmvArgs a,
+                CgState* st, double* partials) {
+    if (st->done) return;
+    extern __shared__ unsigned char spmv_smem_raw[];
+    __shared__ double sm[32];
+    unsigned char* const base = spmv_smem_raw + ((128u - (smem_u32(spmv_smem_raw) & 127u)) & 127u);
+    float(*const S)[kSSh][kSSw] = (float(*)[kSSh][kSSw])(base + kSStages * kSStageBytes);
+    uint64_t* const bars = (uint64_t*)(base + kSBarOff);
+    const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
+    const i64 kit = *(volatile const i64*)&st->iter;
+    const CUtensorMap* pmap = (kit & 1) ? &pmap1 : &pmap0;  // p_old
+    float* const p_new = (kit & 1) ? a.p0 : a.p1;
+    const int first = st->first;
+    const float beta = first ? 0.f : (float)st->beta;
+    if (tid == 0) {
+        for (int s = 0; s < kSStages; ++s) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+        tma_prefetch_map(&zmap);
+        tma_prefetch_map(pmap);
+        tma_prefetch_map(&gmap);
+    }
+    __syncthreads();
+    const float dt = a.dt;
+    const int h = a.h, w = a.w, d = a.d;
+    const int per_plane = a.tiles_x * a.tiles_y;
+    auto stage = [&](unsigned j) -> const unsigned char* { return base + (j % kSStages) * kSStageBytes; };
+    auto Zv = [](const unsigned char* P, int r, int c) -> float { return ((const float*)P)[r * kSVw + c]; };
+    auto Pv = [](const unsigned char* P, int r, int c) -> float {
+        return ((const float*)(P + kSPOff))[r * kSVw + c];
+    };
+    auto Gv = [](const unsigned char* P, int r, int c) -> unsigned { return (P + kSGOff)[r * kSGw + c]; };
+    unsigned issued_end = 0;
+    auto issue = [&](unsigned j, int plane, int x0, int y0) {
+        issued_end = j + 1;
+        unsigned char* dst = base + (j % kSStages) * kSStageBytes;
+        uint64_t* bar = &bars[j % kSStages];
+        mbar_expect_tx(bar, kSTx);
+        tma_load_3d(dst, &zmap, bar, x0 - 4, y0 - 1, plane);
+        tma_load_3d(dst + kSPOff, pmap, bar, x0 - 4, y0 - 1, plane);
+        tma_load_3d(dst + kSGOff, &gmap, bar, x0 - 16, y0, plane);
+    };
+    bool ok = true;
+    auto wait = [&](unsigned j) {
+        if (tid == 0 && ok) ok = mbar_wait(&bars[j % kSStages], (j / kSStages) & 1);
+    };
+    // p_new of cell (yl, xl) of the staged plane P (tile coordinates)
+    auto pn = [&](const unsigned char* P, int yl, int xl) -> float {
+        const float z = Zv(P, yl + 1, xl + 4);
+        return first ? z : fmaf(beta, Pv(P, yl + 1, xl + 4), z);
+    };
+    unsigned seq = 0;
+    bool failed = false;
+    Acc<float> acc;
+    for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
+        const int tz = item / per_plane, t2 = item - tz * per_plane;
+        const int x0 = (t2 % a.tiles_x) * kSX, y0 = (t2 / a.tiles_x) * kSY;
+        const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
+        const int n = z1 - z0 + 2;  // planes z0 - 1 .. z1 (ring index j = plane - z0 + 1)
+        if (tid == 0)
+            for (int j = 0; j < min(n, kSStages); ++j) issue(seq + j, z0 - 1 + j, x0, y0);
+        // p_new of plane x (tile and ring) into its slot; the tile's values
+        // are stored when x is one of this chunk's planes
+        auto fill = [&](const unsigned char* P, int x) {
+            float(*const D)[kSSw] = S[x & 3];
+#pragma unroll
+            for (int r = 0; r < kSRows; ++r) {
+                const int yl = ty + r * kSWarps, xl = 2 * lane;
+                const float v0 = pn(P, yl, xl), v1 = pn(P, yl, xl + 1);
+                D[yl + 1][xl + 1] = v0;
+                D[yl + 1][xl + 2] = v1;
+                const int gy = y0 + yl, gx = x0 + xl;
+                if (x >= z0 && x < z1 && gy < h && gx < w)
+                    *(float2*)(p_new + ((i64)x * h + gy) * w + gx) = make_float2(v0, v1);
+            }
+            if (tid < 64) {  // ring rows y0 - 1 and y0 + kSY
+                const int yl = tid < 32 ? -1 : kSY, xl = 2 * lane;
+                D[yl + 1][xl + 1] = pn(P, yl, xl);
+                D[yl + 1][xl + 2] = pn(P, yl, xl + 1);
+            } else if (tid < 64 + 2 * kSY) {  // ring columns x0 - 1 and x0 + kSX
+                const int k = tid - 64;
+                const int xl = k < kSY ? -1 : kSX, yl = k < kSY ? k : k - kSY;
+                D[yl + 1][xl + 1] = pn(P, yl, xl);
+            }
+        };
+        wait(seq);
+        wait(seq + 1);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        fill(stage(seq), z0 - 1);
+        for (int i = 0; i <= z1 - z0; ++i) {
+            const int q = z0 - 1 + i;  // Ap of plane q after p_new of plane q + 1
+            fill(stage(seq + i + 1), q + 1);
+            if (i + 2 < n) wait(seq + i + 2);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            // plane q - 1's stage has served its p_new and its flags
+            if (tid == 0 && i >= 1 && i - 1 + kSStages < n) issue(seq + i - 1 + kSStages, z0 - 2 + i + kSStages, x0, y0);
+            if (i >= 1) {
+                const unsigned char* P = stage(seq + i);
+#pragma unroll
+                for (int r = 0; r < kSRows; ++r) {
+                    const int yl = ty + r * kSWarps, gy = y0 + yl;
+                    float out[2];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int xl = 2 * lane + u;
+                        const unsigned f = Gv(P, yl, xl + 16);
+                        const float pc = S[q & 3][yl + 1][xl + 1];
+                        const float gy_lo = (f & YLO) ? -sub_rn(pc, S[q & 3][yl][xl + 1]) : 0.f;
+                        const float gy_hi = (f & YHI) ? -sub_rn(S[q & 3][yl + 2][xl + 1], pc) : 0.f;
+                        const float gx_lo = (f & XLO) ? sub_rn(S[q & 3][yl + 1][xl], pc) : 0.f;
+                        const float gx_hi = (f & XHI) ? sub_rn(pc, S[q & 3][yl + 1][xl + 2]) : 0.f;
+                        float v = add_rn(sub_rn(sub_rn(gy_hi, gy_lo), gx_lo), gx_hi);
+                        const float gz_lo = (f & ZLO) ? -sub_rn(pc, S[(q - 1) & 3][yl + 1][xl + 1]) : 0.f;
+                        const float gz_hi = (f & ZHI) ? -sub_rn(S[(q + 1) & 3][yl + 1][xl + 1], pc) : 0.f;
+                        v = add_rn(sub_rn(v, gz_lo), gz_hi);
+                        out[u] = mul_rn(v, dt);
+                    }
+                    const int gx = x0 + 2 * lane;
+                    if (gy < h && gx < w) {
+                        *(float2*)(a.ap + ((i64)q * h + gy) * w + gx) = make_float2(out[0], out[1]);
+                        acc.add(S[q & 3][yl + 1][2 * lane + 1] * out[0]);
+                        acc.add(S[q & 3][yl + 1][2 * lane + 2] * out[1]);
+                    }
+                }
+            }
+        }
+        if (failed) break;
+        __syncthreads();  // every thread is done with the ring before the next item's loads
+        seq += n;
+    }
+    if (failed) {  // a plane never arrived: drain the copies in flight (bounded), stop the solve
+        if (tid == 0) {
+            const uint64_t t0 = global_ns();
+            for (unsigned j = issued_end > kSStages ? issued_end - kSStages : 0; j < issued_end; ++j)
+                while (!mbar_try_wait(&bars[j % kSStages], (j / kSStages) & 1) && global_ns() - t0 < kMbarWaitNs) {
+                }
+            st->status = PG_TIMEOUT;
+            st->done = 1;
+        }
+        return;
+    }
+    const double s = block_sum<kSThreads>(acc.value(), sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    if (!last_block(&st->counter[1])) return;
+    const double pap = reduce_partials<false, kSThreads>(partials, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+        st->counter[1] = 0;
+        st->pap = pap;
+        if (!isfinite(pap)) {
+            st->status = PG_NAN_DETECTED;
+            st->done = 1;
+        } else if (!(pap > 0.0)) {
+            st->status = st->sigma == 0.0 ? PG_NOT_CONVERGED : PG_BREAKDOWN;
+            st->done = 1;
+        } else {
+            st->alpha = st->sigma / pap;  // pcg.rs:53
+        }
+    }
+}
+
+// Tensor maps by (pointer, element size, box), shared by every grid.
+struct MapCache {
+    std::mutex m;
+    struct E {
+        const void* p = nullptr;
+        Dims D{};
+        int elem = 0, bx = 0, by = 0;
+        CUtensorMap map;
+    } e[16];
+    int next = 0;
+};
+
+MapCache& map_cache() {
+    static MapCache c;
+    return c;
+}
+
+bool cached_map(const void* p, int elem, const Dims& D, int bx, int by, CUtensorMap* out) {
+    MapCache& c = map_cache();
+    std::lock_guard<std::mutex> lk(c.m);
+    for (auto& e : c.e)
+        if (e.p == p && e.elem == elem && e.bx == bx && e.by == by && e.D.d == D.d && e.D.h == D.h && e.D.w == D.w) {
+            *out = e.map;
+            return true;
+        }
+    MapCache::E& e = c.e[c.next];
+    if (!encode_map_3d(&e.map, p, elem, D.w, D.h, D.d, bx, by)) return false;
+    c.next = (c.next + 1) % 16;
+    e.p = p;
+    e.D = D;
+    e.elem = elem;
+    e.bx = bx;
+    e.by = by;
+    *out = e.map;
+    return true;
+}
+
+}  // namespace
+
+bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, float* p1, float* ap,
+                     const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials) {
+    static int cap = -1;
+    if (cap < 0) {
+        cap = 0;
+        if (cudaFuncSetAttribute(k_cg_spmv3p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSSmem) ==
+            cudaSuccess) {
+            int bps = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cg_spmv3p, kSThreads, kSSmem) == cudaSuccess)
+                cap = std::min(bps * num_sms, kMaxBlocks);
+        }
+        cudaGetLastError();
+    }
+    if (cap <= 0 || D.nd != 3 || D.w % 16 != 0 || D.nc() >= ((i64)1 << 31)) return false;
+    if (((uintptr_t)ap & 7) || ((uintptr_t)p0 & 7) || ((uintptr_t)p1 & 7)) return false;
+    CUtensorMap zm, pm0, pm1, gm;
+    if (!cached_map(zb, 4, D, kSVw, kSVh, &zm) || !cached_map(p0, 4, D, kSVw, kSVh, &pm0) ||
+        !cached_map(p1, 4, D, kSVw, kSVh, &pm1) || !cached_map(flags, 1, D, kSGw, kSGh, &gm))
+        return false;
+    SpmvArgs a;
+    a.d = (int)D.d;
+    a.h = (int)D.h;
+    a.w = (int)D.w;
+    a.dt = dt;
+    a.p0 = p0;
+    a.p1 = p1;
+    a.ap = ap;
+    a.tiles_x = (a.w + kSX - 1) / kSX;
+    a.tiles_y = (a.h + kSY - 1) / kSY;
+    const int tiles = a.tiles_x * a.tiles_y;
+    const int nch = std::max(1, std::min(cap / tiles, (a.d + 7) / 8));
+    a.zc = (a.d + nch - 1) / nch;
+    a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
+    const int nb = std::max(1, std::min(a.nwork, cap));
+    k_cg_spmv3p<<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
+    return true;
+}
+
+}  // namespace pg

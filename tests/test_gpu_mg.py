@@ -123,7 +123,7 @@ def test_profile_active_skips_exit_at_entry_launches(pg, oracle):
         st, *_ = solve_case(pg, oracle, (192, 192, 192), False, 2, 1e-5)  # real launches >> exit-at-entry ones
     finally:
         lib.pg_profile_enable(0)
-    k = names.index("cg_spmv")
+    k = names.index("cg_update")  # a plain kernel: its exit-at-entry launches take microseconds
     t, n, ta, na = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
     lib.pg_profile_read(k, C.byref(t), C.byref(n))
     lib.pg_profile_read_active(k, C.byref(ta), C.byref(na))
