@@ -47,30 +47,11 @@ template <class T, int PM> __device__ __forceinline__ T zof(T rv, const uint8_t*
     return rv;
 }
 
-template <class T, int PM>
-__global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ b,
-                                                          const uint8_t* __restrict__ flags, i64 n, T dt, double thr,
-                                                          double rel_tol, i64 max_iter, int zero_x, CgState* st,
-                                                          double* partials) {
-    __shared__ double sm[32];
-    Acc<T> sig;
-    T bm = T(0);
-    int bad = 0;
-    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
-        const T bv = b[c];
-        if (zero_x) x[c] = T(0);
-        r[c] = bv;
-        bm = fmax(bm, fabs(bv));
-        bad |= !isfinite(bv);
-        if (PM != PM_ZBUF) sig.add(zof<T, PM>(bv, flags, c, dt) * bv);
-    }
-    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
-    const double bsum = block_max<kCgThreads>((double)bm, sm);
-    const double ssum = block_sum<kCgThreads>(sig.value(), sm);
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = bsum;
-        partials[kMaxBlocks + blockIdx.x] = ssum;
-    }
+// Last block of the init kernels: ||b||inf, z.r (unless the preconditioner
+// publishes it) and the stop threshold into the CG state.
+template <class T>
+__device__ __forceinline__ void cg_init_finish(CgState* st, double* partials, double* sm, double thr, double rel_tol,
+                                               i64 max_iter) {
     if (!last_block(&st->counter[0])) return;
     const double bmax = reduce_partials<true, kCgThreads>(partials, gridDim.x, sm);
     const double sigma = reduce_partials<false, kCgThreads>(partials + kMaxBlocks, gridDim.x, sm);
@@ -98,6 +79,57 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
             st->done = 1;
         }
     }
+}
+
+template <class T, int PM>
+__global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ b,
+                                                          const uint8_t* __restrict__ flags, i64 n, T dt, double thr,
+                                                          double rel_tol, i64 max_iter, int zero_x, CgState* st,
+                                                          double* partials) {
+    __shared__ double sm[32];
+    Acc<T> sig;
+    T bm = T(0);
+    int bad = 0;
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
+        const T bv = b[c];
+        if (zero_x) x[c] = T(0);
+        r[c] = bv;
+        bm = fmax(bm, fabs(bv));
+        bad |= !isfinite(bv);
+        if (PM != PM_ZBUF) sig.add(zof<T, PM>(bv, flags, c, dt) * bv);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
+    const double bsum = block_max<kCgThreads>((double)bm, sm);
+    const double ssum = block_sum<kCgThreads>(sig.value(), sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bsum;
+        partials[kMaxBlocks + blockIdx.x] = ssum;
+    }
+    cg_init_finish<T>(st, partials, sm, thr, rel_tol, max_iter);
+}
+
+// The init of the MG path on float4 vectors (the V-cycle publishes z.r, so
+// the only reduction is the order-independent ||b||inf); n4 = n / 4.
+__global__ void __launch_bounds__(kCgThreads)
+    k_cg_init4(float4* __restrict__ x, float4* __restrict__ r, const float4* __restrict__ b, i64 n4, double thr,
+               double rel_tol, i64 max_iter, int zero_x, CgState* st, double* partials) {
+    __shared__ double sm[32];
+    float bm = 0.f;
+    int bad = 0;
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n4; c += (i64)gridDim.x * blockDim.x) {
+        const float4 bv = b[c];
+        if (zero_x) x[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r[c] = bv;
+        bm = fmaxf(fmaxf(fmaxf(bm, fabsf(bv.x)), fmaxf(fabsf(bv.y), fabsf(bv.z))), fabsf(bv.w));
+        bad |= !isfinite(bv.x) | !isfinite(bv.y) | !isfinite(bv.z) | !isfinite(bv.w);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
+    const double bsum = block_max<kCgThreads>((double)bm, sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bsum;
+        partials[kMaxBlocks + blockIdx.x] = 0.0;
+    }
+    cg_init_finish<float>(st, partials, sm, thr, rel_tol, max_iter);
 }
 
 // Fused search-direction update and operator application.
@@ -535,7 +567,13 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
     Workspace& ws = g->ws;
     cudaStream_t s = g->stream;
     PG_CUDA(cudaMemsetAsync(ws.state, 0, sizeof(CgState), s));
-    PG_LAUNCH(KK_CG_INIT, s,
+    if (PM == PM_ZBUF && sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.r) && aligned16(buf.b))
+        PG_LAUNCH(KK_CG_INIT, s,
+                  k_cg_init4<<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.b, n / 4,
+                                                       cfg.threshold, cfg.rel_tol, cfg.max_iter, cfg.zero_x,
+                                                       ws.state, ws.partials));
+    else
+        PG_LAUNCH(KK_CG_INIT, s,
               k_cg_init<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.b, g->flags, n, dt, cfg.threshold,
                                                          cfg.rel_tol, cfg.max_iter, cfg.zero_x, ws.state,
                                                          ws.partials));

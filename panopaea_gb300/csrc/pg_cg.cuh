@@ -54,6 +54,13 @@ template <> struct Acc<double> {
 bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, float* p1, float* ap,
                      const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials);
 
+// The double-float residual r = b - A (xh + xl) and ||r||inf (to *out) of the
+// refinement on 3D grids, TMA-staged (pg_spmv.cu); false when it does not
+// apply and nothing was launched.
+bool residual_df_tma_launch(cudaStream_t s, int num_sms, const float* b, const float* xh, const float* xl,
+                            const uint8_t* flags, const Dims& D, float dt, float* r, double* partials,
+                            unsigned int* counter, double* out, CgState* st);
+
 // Hooks for an outer preconditioner that produces z between the update
 // and the next SpMV (multigrid).  The last V-cycle kernel reduces z.r and
 // calls cg_finish_rz on the device state.

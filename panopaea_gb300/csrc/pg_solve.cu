@@ -335,7 +335,13 @@ static int residual64(pg_grid* g, const float* b, const void* x64, bool native, 
         else
             PG_LAUNCH(KK_RESIDUAL64, s, k_residual64<3><<<nb, kThreads, 0, s>>>(b, x, g->flags, D, dt, r, g->ws.partials, counter, dev_out));
     } else {
-        if (D.nd == 2) {
+        bool done = false;
+        if (D.nd == 3)
+            PG_LAUNCH(KK_RESIDUAL64, s,
+                      done = residual_df_tma_launch(s, g->num_sms, b, xh, xl, g->flags, D, (float)dt, r,
+                                                    g->ws.partials, counter, dev_out, g->ws.state));
+        if (done) {
+        } else if (D.nd == 2) {
             PG_LAUNCH(KK_RESIDUAL64, s, k_residual_df<2><<<nb, kThreads, 0, s>>>(b, xh, xl, g->flags, D, (float)dt, r, g->ws.partials, counter, dev_out));
         } else {
             const int tiles_x = (int)((D.w + kRTX - 1) / kRTX), tiles_y = (int)((D.h + kRTY - 1) / kRTY);

@@ -1,6 +1,7 @@
-// pg_spmv.cu -- the fused SpMV of the multigrid-preconditioned CG on 3D
-// grids, TMA-staged (p = z + beta p, Ap, p.Ap; pcg.rs:52-53, 77 with the
-// masked Laplacian of grid.rs).
+// pg_spmv.cu -- TMA-staged z-marching kernels of the 3D solve: the fused
+// SpMV of the multigrid-preconditioned CG (p = z + beta p, Ap, p.Ap;
+// pcg.rs:52-53, 77 with the masked Laplacian of grid.rs) and the
+// double-float residual b - A x of the refinement.
 //
 // A block owns a kSX x kSY column tile and walks a chunk of z planes.  TMA
 // stages every plane of z and p_old (one-cell halo) and of the face flags
@@ -214,6 +215,180 @@ __global__ void __launch_bounds__(kSThreads, 2)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float residual r = b - A (xh + xl), ||r||inf (the refinement's outer
+// residual).  Stages per plane: xh and xl with a one-cell halo, b and the
+// flags on the tile; plane p's residual reads the stages of planes p-1, p,
+// p+1 (its z neighbours are the halo boxes' centres), so a stage is refilled
+// once plane p+1 is done with it.  Same arithmetic as k_residual_df3t.
+constexpr int kRX = 64, kRWarps = 8, kRRows = 2, kRY = kRWarps * kRRows;
+constexpr int kRThreads = 32 * kRWarps;
+constexpr int kRStages = 6;
+constexpr int kRVw = kRX + 8, kRVh = kRY + 2;  // xh / xl boxes from (x0 - 4, y0 - 1)
+constexpr int kRBw = kRX, kRBh = kRY;          // b box from (x0, y0)
+constexpr int kRGw = kRX + 32, kRGh = kRY;     // flags box from (x0 - 16, y0)
+constexpr int kRVBytes = kRVw * kRVh * 4, kRBBytes = kRBw * kRBh * 4, kRGBytes = kRGw * kRGh;
+constexpr int kRVPad = ((kRVBytes + 127) / 128) * 128;
+constexpr int kRLOff = kRVPad, kRBOff = 2 * kRVPad, kRGOff = kRBOff + ((kRBBytes + 127) / 128) * 128;
+constexpr int kRStageBytes = kRGOff + ((kRGBytes + 127) / 128) * 128;
+constexpr int kRBarOff = kRStages * kRStageBytes;
+constexpr size_t kRSmem = 128 + kRBarOff + kRStages * 8;
+constexpr unsigned kRTx = 2 * kRVBytes + kRBBytes + kRGBytes;
+static_assert(kRStageBytes % 128 == 0, "TMA boxes must stay 128-byte aligned");
+
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+struct ResArgs {
+    int d, h, w;
+    float dt;
+    float* r;
+    int tiles_x, tiles_y, zc, nwork;
+};
+
+__global__ void __launch_bounds__(kRThreads, 2)
+    k_residual_df3p(const __grid_constant__ CUtensorMap hmap, const __grid_constant__ CUtensorMap lmap,
+                    const __grid_constant__ CUtensorMap bmap, const __grid_constant__ CUtensorMap gmap, ResArgs a,
+                    double* partials, unsigned int* counter, double* out, CgState* st) {
+    extern __shared__ unsigned char res_smem_raw[];
+    __shared__ double sm[32];
+    unsigned char* const base = res_smem_raw + ((128u - (smem_u32(res_smem_raw) & 127u)) & 127u);
+    uint64_t* const bars = (uint64_t*)(base + kRBarOff);
+    const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
+    if (tid == 0) {
+        for (int s = 0; s < kRStages; ++s) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+        tma_prefetch_map(&hmap);
+        tma_prefetch_map(&lmap);
+        tma_prefetch_map(&bmap);
+        tma_prefetch_map(&gmap);
+    }
+    __syncthreads();
+    const float dt = a.dt;
+    const int h = a.h, w = a.w, d = a.d;
+    const int per_plane = a.tiles_x * a.tiles_y;
+    auto stage = [&](unsigned j) -> const unsigned char* { return base + (j % kRStages) * kRStageBytes; };
+    auto H = [](const unsigned char* P, int r, int c) -> float { return ((const float*)P)[r * kRVw + c]; };
+    auto L = [](const unsigned char* P, int r, int c) -> float { return ((const float*)(P + kRLOff))[r * kRVw + c]; };
+    auto Bv = [](const unsigned char* P, int r, int c) -> float { return ((const float*)(P + kRBOff))[r * kRBw + c]; };
+    auto Gv = [](const unsigned char* P, int r, int c) -> unsigned { return (P + kRGOff)[r * kRGw + c]; };
+    unsigned issued_end = 0;
+    auto issue = [&](unsigned j, int plane, int x0, int y0) {
+        issued_end = j + 1;
+        unsigned char* dst = base + (j % kRStages) * kRStageBytes;
+        uint64_t* bar = &bars[j % kRStages];
+        mbar_expect_tx(bar, kRTx);
+        tma_load_3d(dst, &hmap, bar, x0 - 4, y0 - 1, plane);
+        tma_load_3d(dst + kRLOff, &lmap, bar, x0 - 4, y0 - 1, plane);
+        tma_load_3d(dst + kRBOff, &bmap, bar, x0, y0, plane);
+        tma_load_3d(dst + kRGOff, &gmap, bar, x0 - 16, y0, plane);
+    };
+    bool ok = true;
+    auto wait = [&](unsigned j) {
+        if (tid == 0 && ok) ok = mbar_wait(&bars[j % kRStages], (j / kRStages) & 1);
+    };
+    unsigned seq = 0;
+    bool failed = false;
+    float m = 0.f;
+    for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
+        const int tz = item / per_plane, t2 = item - tz * per_plane;
+        const int x0 = (t2 % a.tiles_x) * kRX, y0 = (t2 / a.tiles_x) * kRY;
+        const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
+        const int n = z1 - z0 + 2;  // planes z0 - 1 .. z1 (ring index j = plane - z0 + 1)
+        if (tid == 0)
+            for (int j = 0; j < min(n, kRStages); ++j) issue(seq + j, z0 - 1 + j, x0, y0);
+        wait(seq);
+        wait(seq + 1);
+        wait(seq + 2);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        for (int i = 0; i < z1 - z0; ++i) {
+            const int p = z0 + i;
+            const unsigned char *Pm = stage(seq + i), *P0 = stage(seq + i + 1), *Pp = stage(seq + i + 2);
+#pragma unroll
+            for (int rr = 0; rr < kRRows; ++rr) {
+                const int yl = ty + rr * kRWarps, gy = y0 + yl;
+                float out2[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int xl = 2 * lane + u;
+                    const unsigned f = Gv(P0, yl, xl + 16);
+                    const float ch = H(P0, yl + 1, xl + 4), cl = L(P0, yl + 1, xl + 4);
+                    float sh = 0.f, sl = 0.f;
+                    auto face = [&](float nh, float nl) {
+                        float dh, de, t, te;
+                        df_two_sum(ch, -nh, dh, de);
+                        df_two_sum(sh, dh, t, te);
+                        sh = t;
+                        sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(te, de), __fsub_rn(cl, nl)));
+                    };
+                    if (f & XLO) face(H(P0, yl + 1, xl + 3), L(P0, yl + 1, xl + 3));
+                    if (f & XHI) face(H(P0, yl + 1, xl + 5), L(P0, yl + 1, xl + 5));
+                    if (f & YLO) face(H(P0, yl, xl + 4), L(P0, yl, xl + 4));
+                    if (f & YHI) face(H(P0, yl + 2, xl + 4), L(P0, yl + 2, xl + 4));
+                    if (f & ZLO) face(H(Pm, yl + 1, xl + 4), L(Pm, yl + 1, xl + 4));
+                    if (f & ZHI) face(H(Pp, yl + 1, xl + 4), L(Pp, yl + 1, xl + 4));
+                    const float ph = __fmul_rn(dt, sh);
+                    const float pl = __fadd_rn(__fmaf_rn(dt, sh, -ph), __fmul_rn(dt, sl));
+                    float rh, re;
+                    df_two_sum(Bv(P0, yl, xl), -ph, rh, re);
+                    out2[u] = __fadd_rn(rh, __fsub_rn(re, pl));
+                }
+                const int gx = x0 + 2 * lane;
+                if (gy < h && gx < w) {
+                    *(float2*)(a.r + ((i64)p * h + gy) * w + gx) = make_float2(out2[0], out2[1]);
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        m = fmaxf(m, fabsf(out2[u]));
+                        if (out2[u] != out2[u]) m = __int_as_float(0x7f800000);
+                    }
+                }
+            }
+            if (i + 3 < n) wait(seq + i + 3);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            // plane p - 1's stage has served its last z neighbour
+            if (tid == 0 && i + kRStages < n) issue(seq + i + kRStages, z0 - 1 + i + kRStages, x0, y0);
+        }
+        if (failed) break;
+        __syncthreads();
+        seq += n;
+    }
+    if (failed) {  // a plane never arrived: drain the copies in flight (bounded), report NaN
+        if (tid == 0) {
+            const uint64_t t0 = global_ns();
+            for (unsigned j = issued_end > kRStages ? issued_end - kRStages : 0; j < issued_end; ++j)
+                while (!mbar_try_wait(&bars[j % kRStages], (j / kRStages) & 1) && global_ns() - t0 < kMbarWaitNs) {
+                }
+            st->status = PG_TIMEOUT;
+        }
+        m = __int_as_float(0x7fc00000);
+    }
+    const double bm = block_max<kRThreads>((double)m, sm);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bm;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v = fmax(v, __ldcg(partials + i));
+    v = block_max<kRThreads>(v, sm);
+    if (threadIdx.x == 0) {
+        *out = v;
+        *counter = 0;
+    }
+}
+
 // Tensor maps by (pointer, element size, box), shared by every grid.
 struct MapCache {
     std::mutex m;
@@ -288,6 +463,42 @@ bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, fl
     a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
     const int nb = std::max(1, std::min(a.nwork, cap));
     k_cg_spmv3p<<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
+    return true;
+}
+
+bool residual_df_tma_launch(cudaStream_t s, int num_sms, const float* b, const float* xh, const float* xl,
+                            const uint8_t* flags, const Dims& D, float dt, float* r, double* partials,
+                            unsigned int* counter, double* out, CgState* st) {
+    static int cap = -1;
+    if (cap < 0) {
+        cap = 0;
+        if (cudaFuncSetAttribute(k_residual_df3p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRSmem) ==
+            cudaSuccess) {
+            int bps = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_residual_df3p, kRThreads, kRSmem) == cudaSuccess)
+                cap = std::min(bps * num_sms, kMaxBlocks);
+        }
+        cudaGetLastError();
+    }
+    if (cap <= 0 || D.nd != 3 || D.w % 16 != 0 || D.nc() >= ((i64)1 << 31) || ((uintptr_t)r & 7)) return false;
+    CUtensorMap hm, lm, bm, gm;
+    if (!cached_map(xh, 4, D, kRVw, kRVh, &hm) || !cached_map(xl, 4, D, kRVw, kRVh, &lm) ||
+        !cached_map(b, 4, D, kRBw, kRBh, &bm) || !cached_map(flags, 1, D, kRGw, kRGh, &gm))
+        return false;
+    ResArgs a;
+    a.d = (int)D.d;
+    a.h = (int)D.h;
+    a.w = (int)D.w;
+    a.dt = dt;
+    a.r = r;
+    a.tiles_x = (a.w + kRX - 1) / kRX;
+    a.tiles_y = (a.h + kRY - 1) / kRY;
+    const int tiles = a.tiles_x * a.tiles_y;
+    const int nch = std::max(1, std::min(cap / tiles, (a.d + 7) / 8));
+    a.zc = (a.d + nch - 1) / nch;
+    a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
+    const int nb = std::max(1, std::min(a.nwork, cap));
+    k_residual_df3p<<<nb, kRThreads, kRSmem, s>>>(hm, lm, bm, gm, a, partials, counter, out, st);
     return true;
 }
 
