@@ -38,9 +38,9 @@ __global__ void k_advect_3d(T* __restrict__ dst, const T* __restrict__ q, const 
     GRID_STRIDE(i, d * hw) {
         const I zy = i / w, x = i - zy * w;
         const I z = zy / h, y = zy - z * h;
-        const T vcx = div_rn(add_rn(vel[FX(z, y, x)], vel[FX(z, y, x + 1)]), T(2));
-        const T vcy = div_rn(add_rn(vel[FY(z, y, x)], vel[FY(z, y + 1, x)]), T(2));
-        const T vcz = div_rn(add_rn(vel[FZ(z, y, x)], vel[FZ(z + 1, y, x)]), T(2));
+        const T vcx = half_rn(add_rn(vel[FX(z, y, x)], vel[FX(z, y, x + 1)]));
+        const T vcy = half_rn(add_rn(vel[FY(z, y, x)], vel[FY(z, y + 1, x)]));
+        const T vcz = half_rn(add_rn(vel[FZ(z, y, x)], vel[FZ(z + 1, y, x)]));
         const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
         const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
         const T ppz = back(add_rn((T)z, T(0.5)), ndt, vcz);
@@ -203,8 +203,8 @@ __device__ __forceinline__ void corner_range(const T* __restrict__ q, const T* _
         const T* vy = vel;
         const T* vx = vel + (h + 1) * w;
         const I y = i / w, x = i - y * w;
-        const T vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), T(2));
-        const T vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), T(2));
+        const T vcx = half_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]));
+        const T vcy = half_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]));
         I ix, iy;
         T u, v;
         cell_coord(back(add_rn((T)x, T(0.5)), ndt, vcx), w, hix, ix, u);
@@ -218,9 +218,9 @@ __device__ __forceinline__ void corner_range(const T* __restrict__ q, const T* _
     const I offy = (I)D.offy(), offx = (I)D.offx();
     const I zy = i / w, x = i - zy * w;
     const I z = zy / h, y = zy - z * h;
-    const T vcx = div_rn(add_rn(vel[offx + (z * h + y) * (w + 1) + x], vel[offx + (z * h + y) * (w + 1) + x + 1]), T(2));
-    const T vcy = div_rn(add_rn(vel[offy + (z * (h + 1) + y) * w + x], vel[offy + (z * (h + 1) + y + 1) * w + x]), T(2));
-    const T vcz = div_rn(add_rn(vel[(z * h + y) * w + x], vel[((z + 1) * h + y) * w + x]), T(2));
+    const T vcx = half_rn(add_rn(vel[offx + (z * h + y) * (w + 1) + x], vel[offx + (z * h + y) * (w + 1) + x + 1]));
+    const T vcy = half_rn(add_rn(vel[offy + (z * (h + 1) + y) * w + x], vel[offy + (z * (h + 1) + y + 1) * w + x]));
+    const T vcz = half_rn(add_rn(vel[(z * h + y) * w + x], vel[((z + 1) * h + y) * w + x]));
     I ix, iy, iz;
     T s, t, u;
     cell_coord(back(add_rn((T)x, T(0.5)), ndt, vcx), w, hix, ix, s);

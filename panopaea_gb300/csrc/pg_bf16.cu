@@ -32,8 +32,8 @@ __global__ void k_advect_bf16_2d(uint16_t* __restrict__ dst, const uint16_t* __r
     const float* vx = vel + (h + 1) * w;
     GRID_STRIDE_B(i, h * w) {
         const I y = i / w, x = i - y * w;
-        const float vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), 2.f);
-        const float vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), 2.f);
+        const float vcx = half_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]));
+        const float vcy = half_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]));
         I ix, iy;
         float u, v;
         cell_coord(back(add_rn((float)x, 0.5f), ndt, vcx), w, hix, ix, u);
@@ -51,9 +51,9 @@ __global__ void k_advect_bf16_3d(uint16_t* __restrict__ dst, const uint16_t* __r
     GRID_STRIDE_B(i, d * hw) {
         const I zy = i / w, x = i - zy * w;
         const I z = zy / h, y = zy - z * h;
-        const float vcx = div_rn(add_rn(vel[offx + (z * h + y) * (w + 1) + x], vel[offx + (z * h + y) * (w + 1) + x + 1]), 2.f);
-        const float vcy = div_rn(add_rn(vel[offy + (z * (h + 1) + y) * w + x], vel[offy + (z * (h + 1) + y + 1) * w + x]), 2.f);
-        const float vcz = div_rn(add_rn(vel[(z * h + y) * w + x], vel[((z + 1) * h + y) * w + x]), 2.f);
+        const float vcx = half_rn(add_rn(vel[offx + (z * h + y) * (w + 1) + x], vel[offx + (z * h + y) * (w + 1) + x + 1]));
+        const float vcy = half_rn(add_rn(vel[offy + (z * (h + 1) + y) * w + x], vel[offy + (z * (h + 1) + y + 1) * w + x]));
+        const float vcz = half_rn(add_rn(vel[(z * h + y) * w + x], vel[((z + 1) * h + y) * w + x]));
         I ix, iy, iz;
         float s, t, u;
         cell_coord(back(add_rn((float)x, 0.5f), ndt, vcx), w, hix, ix, s);

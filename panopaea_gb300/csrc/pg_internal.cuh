@@ -47,6 +47,11 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+// x / 2 and x / 4 as multiplications by the exact reciprocals: both round
+// the same real number, so the result is the IEEE quotient bit for bit, in
+// one instruction instead of a division sequence.
+template <class T> __device__ __forceinline__ T half_rn(T x) { return mul_rn(x, T(0.5)); }
+template <class T> __device__ __forceinline__ T quarter_rn(T x) { return mul_rn(x, T(0.25)); }
 
 // math/interp.rs:7-12: a0*(1-s) + a1*s
 template <class T> __device__ __forceinline__ T lerp_ref(T a0, T a1, T s) {

@@ -40,15 +40,15 @@ template <class T, class I> __device__ __forceinline__ void face_coord(T pos, T 
 template <class T> __device__ __forceinline__ T back(T pos, T ndt, T v) { return add_rn(pos, mul_rn(ndt, v)); }
 
 template <class T> __device__ __forceinline__ T avg4(T a, T b, T c, T d) {
-    return div_rn(add_rn(add_rn(add_rn(a, b), c), d), T(4));
+    return quarter_rn(add_rn(add_rn(add_rn(a, b), c), d));
 }
 
 // advect (dec_fluid.rs:173-211) at cell (y, x); vy = vel, vx = vel + (h+1)w.
 template <class T, class I>
 __device__ __forceinline__ T advect2d_at(const T* __restrict__ q, const T* __restrict__ vy, const T* __restrict__ vx,
                                          I h, I w, T ndt, T hix, T hiy, I y, I x) {
-    const T vcx = div_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]), T(2));
-    const T vcy = div_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]), T(2));
+    const T vcx = half_rn(add_rn(vx[y * (w + 1) + x], vx[y * (w + 1) + x + 1]));
+    const T vcy = half_rn(add_rn(vy[y * w + x], vy[(y + 1) * w + x]));
     const T ppx = back(add_rn((T)x, T(0.5)), ndt, vcx);
     const T ppy = back(add_rn((T)y, T(0.5)), ndt, vcy);
     I ix, iy;
@@ -66,9 +66,8 @@ __device__ __forceinline__ T advect_mac2d_x_at(const T* __restrict__ qx, const T
     const I wx = w + 1;
     const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
     const T velx = vx[y * wx + x];
-    const T vely = div_rn(add_rn(add_rn(add_rn(vy[y * w + xc], vy[(y + 1) * w + xc]), vy[y * w + xm]),
-                                 vy[(y + 1) * w + xm]),
-                          T(4));
+    const T vely = quarter_rn(add_rn(add_rn(add_rn(vy[y * w + xc], vy[(y + 1) * w + xc]), vy[y * w + xm]),
+                                 vy[(y + 1) * w + xm]));
     const T ppx = back(add_rn((T)x, T(0)), ndt, velx);
     const T ppy = back(add_rn((T)y, T(0.5)), ndt, vely);
     I x0, x1, y0, y1;
@@ -84,9 +83,8 @@ __device__ __forceinline__ T advect_mac2d_y_at(const T* __restrict__ qy, const T
                                                const T* __restrict__ vx, I h, I w, T ndt, I y, I x) {
     const I wx = w + 1;
     const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
-    const T velx = div_rn(add_rn(add_rn(add_rn(vx[yc * wx + x], vx[yc * wx + x + 1]), vx[ym * wx + x]),
-                                 vx[ym * wx + x + 1]),
-                          T(4));
+    const T velx = quarter_rn(add_rn(add_rn(add_rn(vx[yc * wx + x], vx[yc * wx + x + 1]), vx[ym * wx + x]),
+                                 vx[ym * wx + x + 1]));
     const T vely = vy[y * w + x];
     const T ppx = back(add_rn((T)x, T(0.5)), ndt, velx);
     const T ppy = back(add_rn((T)y, T(0)), ndt, vely);
