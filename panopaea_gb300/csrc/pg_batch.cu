@@ -152,12 +152,14 @@ __global__ void k_b_project(float* __restrict__ vel, const float* __restrict__ p
 // ---------------------------------------------------------------------------
 // CG over all grids (pcg.rs:14-82 per grid)
 
+// PM_ZBUF: r is the MG z buffer, used as z - zm on the fluid cells.
 template <int PM> __device__ __forceinline__ float bz(const float* __restrict__ r, const uint8_t* __restrict__ flags,
-                                                      i64 k, float dt) {
+                                                      i64 k, float dt, float zm = 0.f) {
     if (PM == PM_JACOBI) {
         const int n = __popc((unsigned)flags[k]);
         return n ? r[k] * __frcp_rn((float)n * dt) : 0.f;
     }
+    if (PM == PM_ZBUF) return flags[k] ? r[k] - zm : r[k];
     return r[k];
 }
 
@@ -165,7 +167,7 @@ template <int PM>
 __global__ void k_b_cg_init(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ b,
                             const uint8_t* __restrict__ flags, const GInfo* __restrict__ gi, const Tile* __restrict__ tiles,
                             int ntiles, int tx, int ty, float dt, double* partials) {
-    __shared__ double sm[32];
+    __shared__ F2 sm[64];
     FOR_TILES(tiles, ntiles) {
         const Tile t = tiles[ti];
         const GInfo G = gi[t.grid];
@@ -178,10 +180,11 @@ __global__ void k_b_cg_init(float* __restrict__ x, float* __restrict__ r, const 
             x[c] = 0.f;
             r[c] = bv;
             bm = isfinite(bv) ? fabsf(bv) : __int_as_float(0x7f800000);
-            sig.add(bz<PM>(b, flags, c, dt) * bv);
+            if (PM == PM_ZBUF) sig.add(bv);  // sum(b) for the lazy projection
+            else sig.add(bz<PM>(b, flags, c, dt) * bv);
         }
-        const double m = bmaxr((double)bm, sm);
-        const double s = bsum(sig.value(), sm);
+        double m, s;
+        tmaxsum(bm, f2_of(sig), sm, &m, &s);
         if (threadIdx.x == 0) {
             partials[2 * (i64)ti] = m;
             partials[2 * (i64)ti + 1] = s;
@@ -195,7 +198,8 @@ __global__ void k_b_cg_init(float* __restrict__ x, float* __restrict__ r, const 
 // so beta and sigma are set later (bmg_rz_finalize).
 template <int STAGE>
 __global__ void k_b_finalize(const GInfo* __restrict__ gi, BState* __restrict__ st, const double* __restrict__ partials,
-                             int n, double rel_tol, double thr_abs, int max_iter, int* active, int zbuf = 0) {
+                             int n, double rel_tol, double thr_abs, int max_iter, int* active, int zbuf = 0,
+                             const double* __restrict__ nfluid = nullptr) {
     __shared__ double sm[32];
     const int g = blockIdx.x;
     if (g >= n) return;
@@ -218,11 +222,16 @@ __global__ void k_b_finalize(const GInfo* __restrict__ gi, BState* __restrict__ 
         S.sigma = bb;
         S.thr = (double)(float)(rel_tol > 0.0 ? rel_tol * a : thr_abs);
         S.beta = 0.0;
+        S.fbeta = 0.f;
+        S.fzm = 0.f;
         S.iter = 0;
         S.max_iter = max_iter;
         S.first = 1;
         S.done = 0;
         S.status = PG_NOT_CONVERGED;
+        S.rsum = bb;
+        S.zmean = 0.0;
+        S.nfluid = nfluid ? nfluid[g] : 0.0;
         if (!isfinite(a) || !isfinite(bb)) {
             S.status = PG_NAN_DETECTED;
             S.done = 1;
@@ -243,6 +252,7 @@ __global__ void k_b_finalize(const GInfo* __restrict__ gi, BState* __restrict__ 
             S.done = 1;
         } else {
             S.alpha = S.sigma / a;
+            S.falpha = (float)S.alpha;
         }
     } else {
         S.iter += 1;
@@ -256,7 +266,10 @@ __global__ void k_b_finalize(const GInfo* __restrict__ gi, BState* __restrict__ 
         } else {
             if (!zbuf) {
                 S.beta = bb / S.sigma;
+                S.fbeta = (float)S.beta;
                 S.sigma = bb;
+            } else {
+                S.rsum = bb;
             }
             S.first = 0;
             if (S.iter >= S.max_iter) S.done = 1;
@@ -272,19 +285,22 @@ template <int PM, int FUSED>
 __global__ void k_b_spmv(const float* __restrict__ r, float* p0, float* p1, float* __restrict__ ap,
                          const uint8_t* __restrict__ flags, const GInfo* __restrict__ gi, const Tile* __restrict__ tiles,
                          int ntiles, int tx, int ty, float dt, const BState* __restrict__ st, double* partials) {
-    __shared__ double sm[32];
+    __shared__ F2 sm[32];
     FOR_TILES(tiles, ntiles) {
         const Tile t = tiles[ti];
         const BState& S = st[t.grid];
         if (S.done) continue;  // uniform per block
         const GInfo G = gi[t.grid];
         const int it = S.iter, first = S.first;
-        const float beta = first ? 0.f : (float)S.beta;
+        const float beta = first ? 0.f : S.fbeta;
+        const float zm = PM == PM_ZBUF ? S.fzm : 0.f;
         const float* p_old = (it & 1) ? p1 : p0;
         float* p_new = (it & 1) ? p0 : p1;
-        auto pn = [&](i64 k) -> float {
+        // p_new of cell k; `fluid`: k has an open face (a neighbour behind an
+        // open face always has), the cells the projected z applies to
+        auto pn = [&](i64 k, bool fluid) -> float {
             if (!FUSED) return p_new[k];
-            const float z = bz<PM>(r, flags, k, dt);
+            const float z = PM == PM_ZBUF ? (fluid ? r[k] - zm : r[k]) : bz<PM>(r, flags, k, dt);
             return first ? z : z + beta * p_old[k];
         };
         const int xx = t.x0 + (int)threadIdx.x % tx, yy = t.y0 + (int)threadIdx.x / tx;
@@ -292,17 +308,17 @@ __global__ void k_b_spmv(const float* __restrict__ r, float* p0, float* p1, floa
         if (xx < G.w && yy < G.h) {
             const i64 c = G.coff + (i64)yy * G.w + xx;
             const uint8_t f = flags[c];
-            const float pc = pn(c);
+            const float pc = pn(c, f != 0);
             if (FUSED) p_new[c] = pc;
-            const float gy_lo = (f & YLO) ? -sub_rn(pc, pn(c - G.w)) : 0.f;
-            const float gy_hi = (f & YHI) ? -sub_rn(pn(c + G.w), pc) : 0.f;
-            const float gx_lo = (f & XLO) ? sub_rn(pn(c - 1), pc) : 0.f;
-            const float gx_hi = (f & XHI) ? sub_rn(pc, pn(c + 1)) : 0.f;
+            const float gy_lo = (f & YLO) ? -sub_rn(pc, pn(c - G.w, true)) : 0.f;
+            const float gy_hi = (f & YHI) ? -sub_rn(pn(c + G.w, true), pc) : 0.f;
+            const float gx_lo = (f & XLO) ? sub_rn(pn(c - 1, true), pc) : 0.f;
+            const float gx_hi = (f & XHI) ? sub_rn(pc, pn(c + 1, true)) : 0.f;
             const float a = mul_rn(add_rn(sub_rn(sub_rn(gy_hi, gy_lo), gx_lo), gx_hi), dt);
             ap[c] = a;
             acc.add(pc * a);
         }
-        const double s = bsum(acc.value(), sm);
+        const double s = tsum(f2_of(acc), sm);
         if (threadIdx.x == 0) {
             partials[2 * (i64)ti] = s;
             partials[2 * (i64)ti + 1] = 0.0;
@@ -325,8 +341,8 @@ __global__ void k_b_pupdate(const float* __restrict__ r, float* p0, float* p1, c
             const i64 c = G.coff + (i64)yy * G.w + xx;
             const float* p_old = (S.iter & 1) ? p1 : p0;
             float* p_new = (S.iter & 1) ? p0 : p1;
-            const float z = bz<PM>(r, flags, c, dt);
-            p_new[c] = S.first ? z : z + (float)S.beta * p_old[c];
+            const float z = bz<PM>(r, flags, c, dt, PM == PM_ZBUF ? S.fzm : 0.f);
+            p_new[c] = S.first ? z : z + S.fbeta * p_old[c];
         }
     }
 }
@@ -336,14 +352,14 @@ __global__ void k_b_update(float* __restrict__ x, float* __restrict__ r, const f
                            const float* __restrict__ ap, const uint8_t* __restrict__ flags, const GInfo* __restrict__ gi,
                            const Tile* __restrict__ tiles, int ntiles, int tx, int ty, float dt,
                            const BState* __restrict__ st, double* partials) {
-    __shared__ double sm[32];
+    __shared__ F2 sm[64];
     FOR_TILES(tiles, ntiles) {
         const Tile t = tiles[ti];
         const BState& S = st[t.grid];
         if (S.done) continue;
         const GInfo G = gi[t.grid];
         const float* p = ((S.iter + 1) & 1) ? p1 : p0;
-        const float alpha = (float)S.alpha;
+        const float alpha = S.falpha;
         const int xx = t.x0 + (int)threadIdx.x % tx, yy = t.y0 + (int)threadIdx.x / tx;
         float rm = 0.f;
         Acc<float> rz;
@@ -358,10 +374,11 @@ __global__ void k_b_update(float* __restrict__ x, float* __restrict__ r, const f
                 const int nn = __popc((unsigned)flags[c]);
                 z = nn ? rv * __frcp_rn((float)nn * dt) : 0.f;
             }
-            rz.add(z * rv);
+            if (PM == PM_ZBUF) rz.add(rv);  // sum(r) for the lazy projection
+            else rz.add(z * rv);
         }
-        const double m = bmaxr((double)rm, sm);
-        const double s = bsum(rz.value(), sm);
+        double m, s;
+        tmaxsum(rm, f2_of(rz), sm, &m, &s);
         if (threadIdx.x == 0) {
             partials[2 * (i64)ti] = m;
             partials[2 * (i64)ti + 1] = s;
@@ -426,20 +443,20 @@ template <int PM> static void b_iter(pg_batch* B, cudaStream_t s, float dt, floa
         const int nt = B->tx * B->ty, nb = bblocks(B, B->ntiles);
         if (B->fused) {
             PG_LAUNCH(KK_CG_SPMV, s,
-                      k_b_spmv<PM_NONE, 1><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
+                      k_b_spmv<PM_ZBUF, 1><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
                                                              B->ntiles, B->tx, B->ty, dt, B->state, B->partials));
         } else {
             PG_LAUNCH(KK_CG_SPMV, s,
-                      k_b_pupdate<PM_NONE><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->flags, B->ginfo, B->tiles, B->ntiles,
+                      k_b_pupdate<PM_ZBUF><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->flags, B->ginfo, B->tiles, B->ntiles,
                                                              B->tx, B->ty, dt, B->state));
             PG_LAUNCH(KK_CG_SPMV, s,
-                      k_b_spmv<PM_NONE, 0><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
+                      k_b_spmv<PM_ZBUF, 0><<<nb, nt, 0, s>>>(B->z, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
                                                              B->ntiles, B->tx, B->ty, dt, B->state, B->partials));
         }
         PG_LAUNCH(KK_STEP_MISC, s,
                   k_b_finalize<1><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n, 0.0, 0.0, 0, B->active));
         PG_LAUNCH(KK_CG_UPDATE, s,
-                  k_b_update<PM_NONE><<<nb, nt, 0, s>>>(x, B->r, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
+                  k_b_update<PM_ZBUF><<<nb, nt, 0, s>>>(x, B->r, B->p0, B->p1, B->ap, B->flags, B->ginfo, B->tiles,
                                                         B->ntiles, B->tx, B->ty, dt, B->state, B->partials));
         PG_LAUNCH(KK_STEP_MISC, s,
                   k_b_finalize<2><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n, 0.0, 0.0, 0, B->active, 1));
@@ -519,15 +536,16 @@ static int b_solve(pg_batch* B, const pg_solver_params* prm, float dt, float* x,
     cudaStream_t s = B->stream;
     const int nt = B->tx * B->ty, nb = bblocks(B, B->ntiles);
     const int nsmooth = prm->mg_smooth > 0 ? prm->mg_smooth : 2;
-    constexpr int PMI = PM == PM_ZBUF ? PM_NONE : PM;  // init: r = b (z comes from the V-cycle)
+    // init: r = b (PM_ZBUF: z comes from the V-cycle; sum(b) for the lazy projection)
     PG_CUDA(cudaMemsetAsync(B->active, 0, sizeof(int), s));
     PG_LAUNCH(KK_CG_INIT, s,
-              k_b_cg_init<PMI><<<nb, nt, 0, s>>>(x, B->r, B->b, B->flags, B->ginfo, B->tiles, B->ntiles, B->tx, B->ty,
-                                                 dt, B->partials));
+              k_b_cg_init<PM><<<nb, nt, 0, s>>>(x, B->r, B->b, B->flags, B->ginfo, B->tiles, B->ntiles, B->tx, B->ty,
+                                                dt, B->partials));
     PG_LAUNCH(KK_STEP_MISC, s,
               k_b_finalize<0><<<B->n, 128, 0, s>>>(B->ginfo, B->state, B->partials, B->n,
                                                    prm->rel_stop ? prm->rel_tol : 0.0, prm->threshold,
-                                                   (int)std::min<i64>(prm->max_iter, 1 << 30), B->active));
+                                                   (int)std::min<i64>(prm->max_iter, 1 << 30), B->active, 0,
+                                                   PM == PM_ZBUF ? B->nfluid : nullptr));
     if (PM == PM_ZBUF) {
         bmg_vcycle(B, s, nsmooth);
         bmg_rz_finalize(B, s, 1);
@@ -663,7 +681,7 @@ int pg_batch_destroy(pg_batch* B) {
     if (B->graph) cudaGraphDestroy(B->graph);
     bmg_release(B);
     void* ptrs[] = {B->ginfo, B->flags, B->face_solid, B->state, B->active, B->partials, B->r, B->ap, B->p0,
-                    B->p1, B->b, B->tmp, B->vtmp, B->tiles, B->tiles_ext, B->z};
+                    B->p1, B->b, B->tmp, B->vtmp, B->tiles, B->tiles_ext, B->z, B->nfluid};
     for (void* p : ptrs) cudaFree(p);
     delete B;
     return PG_OK;
@@ -690,6 +708,11 @@ int pg_batch_set_solid_cells(pg_batch* B, const uint8_t* cs) {
     b_flags(B, cs, flags, fsolid);
     PG_CUDA(cudaStreamSynchronize(B->stream));
     PG_CUDA(cudaMemcpy(B->flags, flags.data(), flags.size(), cudaMemcpyHostToDevice));
+    std::vector<double> nfl(B->n, 0.0);  // fluid cells per grid (the MG path's lazy projection)
+    for (int g = 0; g < B->n; ++g)
+        for (i64 c = B->coff[g]; c < B->coff[g + 1]; ++c) nfl[g] += flags[c] != 0;
+    if (!B->nfluid) PG_CUDA(cudaMalloc(&B->nfluid, sizeof(double) * B->n));
+    PG_CUDA(cudaMemcpy(B->nfluid, nfl.data(), sizeof(double) * B->n, cudaMemcpyHostToDevice));
     if (cs) {
         if (!B->face_solid) PG_CUDA(cudaMalloc(&B->face_solid, (size_t)B->nfaces));
         PG_CUDA(cudaMemcpy(B->face_solid, fsolid.data(), fsolid.size(), cudaMemcpyHostToDevice));

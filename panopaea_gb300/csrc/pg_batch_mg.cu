@@ -127,7 +127,7 @@ template <bool L0, int MODE, bool RZ>
 __global__ void __launch_bounds__(kSmTX * kSmTY)
     k_bmg_smooth(BLv v, const Tile* __restrict__ tiles, int ntiles, int color, const BState* __restrict__ st,
                  double* __restrict__ partials) {
-    __shared__ double sm[32];
+    __shared__ F2 sm[64];
     FOR_TILES(tiles, ntiles) {
         const Tile t = tiles[ti];
         if (st[t.grid].done) continue;  // uniform per block
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kSmTX * kSmTY)
         const int iy = threadIdx.x / kSmTX, ix = threadIdx.x % kSmTX;
         const int y = t.y0 + iy;
         const int x = t.x0 + 2 * ix + ((y + color) & 1);
-        Acc<float> acc;
+        Acc<float> acc, zs;  // z.r and sum(z) (RZ)
         if (y < L.h && x < L.w) {
             const i64 c = L.off + (i64)y * L.w + x;
             if (upd) {
@@ -153,16 +153,24 @@ __global__ void __launch_bounds__(kSmTX * kSmTY)
                     v.e[c] = s * cl.inv;
                 }
             }
-            if (RZ) acc.add(v.e[c] * v.f[c]);
+            if (RZ) {
+                acc.add(v.e[c] * v.f[c]);
+                zs.add(v.e[c]);
+            }
         }
         if (RZ) {
             const int xo = t.x0 + 2 * ix + ((y + color + 1) & 1);
             if (y < L.h && xo < L.w) {
                 const i64 c = L.off + (i64)y * L.w + xo;
                 acc.add(v.e[c] * v.f[c]);
+                zs.add(v.e[c]);
             }
-            const double s = bsum(acc.value(), sm);
-            if (threadIdx.x == 0) partials[ti] = s;
+            double a, b;
+            tsum2(f2_of(acc), f2_of(zs), sm, &a, &b);
+            if (threadIdx.x == 0) {
+                partials[2 * (i64)ti] = a;
+                partials[2 * (i64)ti + 1] = b;
+            }
         }
     }
 }
@@ -296,10 +304,20 @@ __global__ void k_bmg_rz_finalize(const BLevel* __restrict__ info0, BState* __re
     BState& S = st[g];
     if (S.done) return;
     const BLevel L = info0[g];
-    double a = 0.0;
-    for (int t = L.t0 + threadIdx.x; t < L.t1; t += blockDim.x) a += partials[t];
+    double a = 0.0, zsum = 0.0;
+    for (int t = L.t0 + threadIdx.x; t < L.t1; t += blockDim.x) {
+        a += partials[2 * (i64)t];
+        zsum += partials[2 * (i64)t + 1];
+    }
     a = bsum(a, sm);
+    zsum = bsum(zsum, sm);
     if (threadIdx.x != 0) return;
+    if (S.nfluid > 0.0) {  // z stands for z - m on the fluid cells: (z - m).r = z.r - m sum(r)
+        const double m = zsum / S.nfluid;
+        S.zmean = m;
+        S.fzm = (float)m;
+        a -= m * S.rsum;
+    }
     if (!isfinite(a)) {
         S.status = PG_NAN_DETECTED;
         S.done = 1;
@@ -309,6 +327,7 @@ __global__ void k_bmg_rz_finalize(const BLevel* __restrict__ info0, BState* __re
         S.sigma = a;
     } else {
         S.beta = a / S.sigma;
+        S.fbeta = (float)S.beta;
         S.sigma = a;
     }
 }
@@ -450,7 +469,7 @@ static int bmg_build(pg_batch* B, float dt) {
                 (rc = dalloc((void**)&M->f[l], b)))
                 return rc;
         }
-        if (l == 0 && (rc = dalloc((void**)&M->partials, sizeof(double) * st.size()))) return rc;
+        if (l == 0 && (rc = dalloc((void**)&M->partials, 2 * sizeof(double) * st.size()))) return rc;
     }
     std::vector<CoarseInfo> ci(n);
     for (int g = 0; g < n; ++g) {

@@ -28,13 +28,14 @@ template <> __device__ __forceinline__ float rcp_rn<float>(float v) { return __f
 template <> __device__ __forceinline__ double rcp_rn<double>(double v) { return __drcp_rn(v); }
 
 // z = M^-1 r at one cell for PM_NONE / PM_JACOBI.
+// zm: the lazily projected mean of z on the fluid cells (PM_ZBUF; 0 = off).
 template <class T, int PM> __device__ __forceinline__ T zval(const T* __restrict__ r, const uint8_t* __restrict__ flags,
-                                                             const T* __restrict__ zb, i64 k, T dt) {
+                                                             const T* __restrict__ zb, i64 k, T dt, T zm = T(0)) {
     if (PM == PM_JACOBI) {
         const int n = __popc((unsigned)flags[k]);
         return n ? r[k] * rcp_rn<T>((T)n * dt) : T(0);
     }
-    if (PM == PM_ZBUF) return zb[k];
+    if (PM == PM_ZBUF) return flags[k] ? zb[k] - zm : zb[k];
     return r[k];
 }
 
@@ -51,7 +52,7 @@ template <class T, int PM> __device__ __forceinline__ T zof(T rv, const uint8_t*
 // publishes it) and the stop threshold into the CG state.
 template <class T>
 __device__ __forceinline__ void cg_init_finish(CgState* st, double* partials, double* sm, double thr, double rel_tol,
-                                               i64 max_iter) {
+                                               i64 max_iter, double nfluid = 0.0) {
     if (!last_block(&st->counter[0])) return;
     const double bmax = reduce_partials<true, kCgThreads>(partials, gridDim.x, sm);
     const double sigma = reduce_partials<false, kCgThreads>(partials + kMaxBlocks, gridDim.x, sm);
@@ -62,7 +63,10 @@ __device__ __forceinline__ void cg_init_finish(CgState* st, double* partials, do
         st->threshold = t;
         st->bmax = bmax;
         st->rmax = bmax;
-        st->sigma = sigma;  // PM_ZBUF: set later by the preconditioner
+        st->sigma = sigma;  // PM_ZBUF: sum(b) here, z.r set later by the preconditioner
+        st->rsum = sigma;
+        st->nfluid = nfluid;
+        st->zmean = 0.0;
         st->beta = 0.0;
         st->iter = 0;
         st->max_iter = max_iter;
@@ -85,7 +89,7 @@ template <class T, int PM>
 __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ b,
                                                           const uint8_t* __restrict__ flags, i64 n, T dt, double thr,
                                                           double rel_tol, i64 max_iter, int zero_x, CgState* st,
-                                                          double* partials) {
+                                                          double* partials, double nfluid = 0.0) {
     __shared__ double sm[32];
     Acc<T> sig;
     T bm = T(0);
@@ -97,6 +101,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
         bm = fmax(bm, fabs(bv));
         bad |= !isfinite(bv);
         if (PM != PM_ZBUF) sig.add(zof<T, PM>(bv, flags, c, dt) * bv);
+        else sig.add(bv);  // sum(b) for the lazy projection
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
     const double bsum = block_max<kCgThreads>((double)bm, sm);
@@ -105,31 +110,34 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
         partials[blockIdx.x] = bsum;
         partials[kMaxBlocks + blockIdx.x] = ssum;
     }
-    cg_init_finish<T>(st, partials, sm, thr, rel_tol, max_iter);
+    cg_init_finish<T>(st, partials, sm, thr, rel_tol, max_iter, nfluid);
 }
 
 // The init of the MG path on float4 vectors (the V-cycle publishes z.r, so
 // the only reduction is the order-independent ||b||inf); n4 = n / 4.
 __global__ void __launch_bounds__(kCgThreads)
     k_cg_init4(float4* __restrict__ x, float4* __restrict__ r, const float4* __restrict__ b, i64 n4, double thr,
-               double rel_tol, i64 max_iter, int zero_x, CgState* st, double* partials) {
+               double rel_tol, i64 max_iter, int zero_x, CgState* st, double* partials, double nfluid) {
     __shared__ double sm[32];
     float bm = 0.f;
     int bad = 0;
+    float sb = 0.f;  // sum(b) for the lazy projection (feeds a small correction term)
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n4; c += (i64)gridDim.x * blockDim.x) {
         const float4 bv = b[c];
         if (zero_x) x[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         r[c] = bv;
         bm = fmaxf(fmaxf(fmaxf(bm, fabsf(bv.x)), fmaxf(fabsf(bv.y), fabsf(bv.z))), fabsf(bv.w));
         bad |= !isfinite(bv.x) | !isfinite(bv.y) | !isfinite(bv.z) | !isfinite(bv.w);
+        sb += (bv.x + bv.y) + (bv.z + bv.w);
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
     const double bsum = block_max<kCgThreads>((double)bm, sm);
+    const double ssum = block_sum<kCgThreads>((double)sb, sm);
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = bsum;
-        partials[kMaxBlocks + blockIdx.x] = 0.0;
+        partials[kMaxBlocks + blockIdx.x] = ssum;
     }
-    cg_init_finish<float>(st, partials, sm, thr, rel_tol, max_iter);
+    cg_init_finish<float>(st, partials, sm, thr, rel_tol, max_iter, nfluid);
 }
 
 // Fused search-direction update and operator application.
@@ -146,9 +154,10 @@ __global__ void __launch_bounds__(kCgThreads)
     T* __restrict__ p_new = (k & 1) ? p0 : p1;
     const int first = st->first;
     const T beta = first ? T(0) : (T)st->beta;
+    const T zm = (PM == PM_ZBUF && st->nfluid > 0.0) ? (T)st->zmean : T(0);
     const i64 n = D.nc(), w = D.w, hw = D.h * D.w;
     auto pn = [&](i64 k) -> T {
-        const T z = zval<T, PM>(r, flags, zb, k, dt);
+        const T z = zval<T, PM>(r, flags, zb, k, dt, zm);
         return first ? z : z + beta * p_old[k];
     };
     Acc<T> acc;
@@ -212,8 +221,9 @@ __global__ void __launch_bounds__(kTX * kTY)
     T* __restrict__ p_new = (kit & 1) ? p0 : p1;
     const int first = st->first;
     const T beta = first ? T(0) : (T)st->beta;
+    const T zm = (PM == PM_ZBUF && st->nfluid > 0.0) ? (T)st->zmean : T(0);
     auto pn = [&](i64 k) -> T {
-        const T z = zval<T, PM>(r, flags, zb, k, dt);
+        const T z = zval<T, PM>(r, flags, zb, k, dt, zm);
         return first ? z : z + beta * p_old[k];
     };
     const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
@@ -239,7 +249,7 @@ __global__ void __launch_bounds__(kTX * kTY)
             // this plane's stencil, so their latency overlaps the step.
             T rz = T(0), rp = T(0);
             if (inside && z + 2 < d && z + 1 < z1) {
-                rz = zval<T, PM>(r, flags, zb, c + 2 * hw, dt);
+                rz = zval<T, PM>(r, flags, zb, c + 2 * hw, dt, zm);
                 if (!first) rp = p_old[c + 2 * hw];
             }
             S[ty + 1][tx + 1] = cur;
@@ -336,6 +346,7 @@ __global__ void __launch_bounds__(kCgThreads)
         rm = fmax(rm, fabs(rv));
         bad |= !isfinite(rv);
         if (PM != PM_ZBUF) rz.add(zof<T, PM>(rv, flags, c, dt) * rv);
+        else rz.add(rv);  // sum(r) for the lazy projection
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
     const double m = block_max<kCgThreads>((double)rm, sm);
@@ -360,6 +371,7 @@ __global__ void __launch_bounds__(kCgThreads)
             st->done = 1;
         } else {
             if (PM != PM_ZBUF) cg_finish_rz(st, sigma_new);  // pcg.rs:65-68
+            else st->rsum = sigma_new;
             if (it >= st->max_iter) st->done = 1;          // loop bound, pcg.rs:48
         }
     }
@@ -377,7 +389,7 @@ __global__ void __launch_bounds__(kCgThreads)
     const i64 k = *(volatile const i64*)&st->iter;
     const float4* __restrict__ p = ((k + 1) & 1) ? p1 : p0;
     const float alpha = (float)st->alpha, nalpha = -alpha;
-    float rm = 0.f;
+    float rm = 0.f, rs = 0.f;  // rs: sum(r) for the lazy projection (feeds a small correction term)
     int bad = 0;
     auto one = [&](i64 c) {
         const float4 xv = x[c], pv = p[c], rv = r[c], av = ap[c];
@@ -394,6 +406,7 @@ __global__ void __launch_bounds__(kCgThreads)
         r[c] = ro;
         rm = fmaxf(fmaxf(fmaxf(rm, fabsf(ro.x)), fmaxf(fabsf(ro.y), fabsf(ro.z))), fabsf(ro.w));
         bad |= !isfinite(ro.x) | !isfinite(ro.y) | !isfinite(ro.z) | !isfinite(ro.w);
+        rs += (ro.x + ro.y) + (ro.z + ro.w);
     };
     const i64 stride = (i64)gridDim.x * blockDim.x;
     i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -404,10 +417,16 @@ __global__ void __launch_bounds__(kCgThreads)
     if (c < n4) one(c);
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
     const double m = block_max<kCgThreads>((double)rm, sm);
-    if (threadIdx.x == 0) partials[2 * kMaxBlocks + blockIdx.x] = m;
+    const double rsb = block_sum<kCgThreads>((double)rs, sm);
+    if (threadIdx.x == 0) {
+        partials[2 * kMaxBlocks + blockIdx.x] = m;
+        partials[3 * kMaxBlocks + blockIdx.x] = rsb;
+    }
     if (!last_block(&st->counter[2])) return;
     const double rmax = reduce_partials<true, kCgThreads>(partials + 2 * kMaxBlocks, gridDim.x, sm);
+    const double rsum = reduce_partials<false, kCgThreads>(partials + 3 * kMaxBlocks, gridDim.x, sm);
     if (threadIdx.x == 0) {
+        st->rsum = rsum;
         st->counter[2] = 0;
         const i64 it = st->iter + 1;
         st->iter = it;
@@ -571,12 +590,12 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
         PG_LAUNCH(KK_CG_INIT, s,
                   k_cg_init4<<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.b, n / 4,
                                                        cfg.threshold, cfg.rel_tol, cfg.max_iter, cfg.zero_x,
-                                                       ws.state, ws.partials));
+                                                       ws.state, ws.partials, cfg.nfluid));
     else
         PG_LAUNCH(KK_CG_INIT, s,
               k_cg_init<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.b, g->flags, n, dt, cfg.threshold,
                                                          cfg.rel_tol, cfg.max_iter, cfg.zero_x, ws.state,
-                                                         ws.partials));
+                                                         ws.partials, cfg.nfluid));
     PG_CHECK_LAUNCH();
     if (PM == PM_ZBUF && (rc = hook->apply(g, buf.r, buf.z))) return rc;
     // Device-side loop: one graph launch runs every iteration.

@@ -27,6 +27,7 @@ struct CgConfig {
     double dt;
     int check_every;    // 0 = auto
     int zero_x;         // 1: x = 0 first (pcg.rs:32)
+    double nfluid = 0;  // MG on one fluid component: fluid cells (lazy projection of z); 0 = off
 };
 
 // Per-thread partial sums: compensated FP32 (float fields) or plain FP64
@@ -80,8 +81,16 @@ int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stat
 
 // Device side: fold a freshly reduced z.r into the CG state.  Right after
 // init (iter == 0) it is sigma; afterwards beta = z.r / sigma (pcg.rs:67-68).
-__device__ __forceinline__ void cg_finish_rz(CgState* st, double rz) {
+// With the lazy projection on (nfluid > 0) z stands for z - m on the fluid
+// cells, m = sum(z) / nfluid: (z - m).r = z.r - m sum(r) (r is 0 off the
+// fluid cells).
+__device__ __forceinline__ void cg_finish_rz(CgState* st, double rz, double zsum = 0.0) {
     if (st->done) return;
+    if (st->nfluid > 0.0) {
+        const double m = zsum / st->nfluid;
+        st->zmean = m;
+        rz -= m * st->rsum;
+    }
     if (!isfinite(rz)) {
         st->status = PG_NAN_DETECTED;
         st->done = 1;

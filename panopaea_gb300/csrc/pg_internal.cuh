@@ -107,6 +107,11 @@ struct CgState {
     double rz_new;
     i64 iter;          // operator applications done
     i64 max_iter;
+    // MG on one fluid component: z is used as z - mean(z) over the fluid
+    // cells (the constant mode the coarse sweeps amplify), applied lazily
+    double nfluid;     // fluid cells (0: no projection)
+    double zmean;      // mean of the current z over the fluid cells
+    double rsum;       // sum of the current residual
     int done;          // 1: stop issuing work
     int status;        // pg_status
     int first;         // next p-update is p = z

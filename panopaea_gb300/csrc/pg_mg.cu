@@ -59,6 +59,7 @@ struct MgHierarchy {
     uint64_t id = 0;  // unique per build (CUDA-graph cache key)
     Pockets pockets;  // fluid components (empty when the fluid is connected)
     int tail = 0;     // first level handled by the single-block tail kernel (nlev: none)
+    double nfluid = 0;  // cells with an open face (the lazy projection's count)
     // fine level of 3D grids: fused red-black pairs (k_mg_pair) ping-pong
     // between z and e0b; tensor maps of the flags and of the vectors met
     bool pairs = false;
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kMgThreads)
     const int half = (v.w + 1) >> 1;
     const int nrow = v.d * v.h;
     const int total = nrow * half;
-    Acc<float> acc;
+    Acc<float> acc, zs;  // z.r and sum(z) (RZ)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const int row = i / half, k2 = i - row * half;
         const int z = row / v.h, y = row - z * v.h;
@@ -179,7 +180,10 @@ __global__ void __launch_bounds__(kMgThreads)
             }
             const float en = s * cl.inv;
             e[c] = en;
-            if (RZ) acc.add(en * f[c]);
+            if (RZ) {
+                acc.add(en * f[c]);
+                zs.add(en);
+            }
         }
     }
     if (!RZ) return;
@@ -193,15 +197,21 @@ __global__ void __launch_bounds__(kMgThreads)
         if (x < v.w) {
             const int c = row * v.w + x;
             acc.add(e[c] * f[c]);
+            zs.add(e[c]);
         }
     }
     const double s = block_sum<kMgThreads>(acc.value(), sm);
-    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    const double s2 = block_sum<kMgThreads>(zs.value(), sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = s;
+        partials[kMaxBlocks + blockIdx.x] = s2;
+    }
     if (!last_block(&st->counter[3])) return;
     const double rz = reduce_partials<false, kMgThreads>(partials, gridDim.x, sm);
+    const double zsum = reduce_partials<false, kMgThreads>(partials + kMaxBlocks, gridDim.x, sm);
     if (threadIdx.x == 0) {
         st->counter[3] = 0;
-        cg_finish_rz(st, rz);
+        cg_finish_rz(st, rz, zsum);
     }
 }
 
@@ -337,7 +347,7 @@ __global__ void __launch_bounds__(kPThreads, kPMinBlocks)
     };
     unsigned seq = 0;     // planes this block has consumed: ring slot and phase parity
     bool failed = false;  // block-uniform: a wait gave up
-    Acc<float> acc;
+    Acc<float> acc, zs;   // z.r and sum(z) (RZ)
     for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
         const int tz = item / per_plane, t2 = item - tz * per_plane;
         const int x0 = (t2 % a.tiles_x) * kPX, y0 = (t2 / a.tiles_x) * kPY;
@@ -410,6 +420,8 @@ __global__ void __launch_bounds__(kPThreads, kPMinBlocks)
                         if (RZ) {
                             acc.add(e1 * Fv(Pm, yl + 1, xl1 + 4));
                             acc.add(e2 * fv);
+                            zs.add(e1);
+                            zs.add(e2);
                         }
                     }
                 }
@@ -432,12 +444,17 @@ __global__ void __launch_bounds__(kPThreads, kPMinBlocks)
     }
     if (RZ) {
         const double s = block_sum<kPThreads>(acc.value(), sm);
-        if (threadIdx.x == 0) partials[blockIdx.x] = s;
+        const double s2 = block_sum<kPThreads>(zs.value(), sm);
+        if (threadIdx.x == 0) {
+            partials[blockIdx.x] = s;
+            partials[kMaxBlocks + blockIdx.x] = s2;
+        }
         if (last_block(&st->counter[3])) {
             const double rz = reduce_partials<false, kPThreads>(partials, gridDim.x, sm);
+            const double zsum = reduce_partials<false, kPThreads>(partials + kMaxBlocks, gridDim.x, sm);
             if (threadIdx.x == 0) {
                 st->counter[3] = 0;
-                cg_finish_rz(st, rz);
+                cg_finish_rz(st, rz, zsum);
             }
         }
     }
@@ -855,6 +872,9 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
     {
         std::vector<uint8_t> hf((size_t)g->dims.nc());
         PG_CUDA(cudaMemcpy(hf.data(), g->flags, hf.size(), cudaMemcpyDeviceToHost));
+        i64 nf = 0;
+        for (uint8_t f : hf) nf += f != 0;
+        H->nfluid = (double)nf;
         std::vector<i64> cells;
         std::vector<int> start;
         find_pockets(hf.data(), g->dims.nd, g->dims.d, g->dims.h, g->dims.w, 0, cells, start);
@@ -1170,7 +1190,13 @@ int solve_mgpcg(pg_grid* g, const pg_solver_params* prm, const CgConfig& cfg, Cg
     MgHook hook;
     hook.H = H;
     hook.nsmooth = prm->mg_smooth > 0 ? prm->mg_smooth : 2;
-    return run_cg<T>(g, cfg, buf, st, &hook);
+    // One fluid component: z's constant mode on it is removed lazily inside
+    // the CG kernels (the coarse sweeps amplify the constant part that FP32
+    // rounding leaves in r; unremoved, it swamps A p near tight tolerances).
+    // Several components are projected explicitly around the V-cycle.
+    CgConfig c2 = cfg;
+    c2.nfluid = H->pockets.ncomp > 1 ? 0.0 : H->nfluid;
+    return run_cg<T>(g, c2, buf, st, &hook);
 }
 
 template int solve_mgpcg<float>(pg_grid*, const pg_solver_params*, const CgConfig&, CgBuffers<float>, pg_pcg_stats*);

@@ -26,7 +26,7 @@ constexpr int kSX = 64, kSWarps = 8, kSRows = 2, kSY = kSWarps * kSRows;
 constexpr int kSThreads = 32 * kSWarps;
 constexpr int kSStages = 7;
 constexpr int kSVw = kSX + 8, kSVh = kSY + 2;  // z / p_old boxes from (x0 - 4, y0 - 1)
-constexpr int kSGw = kSX + 32, kSGh = kSY;     // flags box from (x0 - 16, y0)
+constexpr int kSGw = kSX + 32, kSGh = kSY + 2;  // flags box from (x0 - 16, y0 - 1)
 constexpr int kSVBytes = kSVw * kSVh * 4;
 constexpr int kSGBytes = kSGw * kSGh;
 constexpr int kSVPad = ((kSVBytes + 127) / 128) * 128;
@@ -89,15 +89,18 @@ __global__ void __launch_bounds__(kSThreads, 2)
         mbar_expect_tx(bar, kSTx);
         tma_load_3d(dst, &zmap, bar, x0 - 4, y0 - 1, plane);
         tma_load_3d(dst + kSPOff, pmap, bar, x0 - 4, y0 - 1, plane);
-        tma_load_3d(dst + kSGOff, &gmap, bar, x0 - 16, y0, plane);
+        tma_load_3d(dst + kSGOff, &gmap, bar, x0 - 16, y0 - 1, plane);
     };
     bool ok = true;
     auto wait = [&](unsigned j) {
         if (tid == 0 && ok) ok = mbar_wait(&bars[j % kSStages], (j / kSStages) & 1);
     };
-    // p_new of cell (yl, xl) of the staged plane P (tile coordinates)
+    // p_new of cell (yl, xl) of the staged plane P (tile coordinates), with
+    // z projected lazily on the fluid cells (zm = 0 when off)
+    const float zm = st->nfluid > 0.0 ? (float)st->zmean : 0.f;
     auto pn = [&](const unsigned char* P, int yl, int xl) -> float {
-        const float z = Zv(P, yl + 1, xl + 4);
+        const float z0 = Zv(P, yl + 1, xl + 4);
+        const float z = Gv(P, yl + 1, xl + 16) ? z0 - zm : z0;
         return first ? z : fmaf(beta, Pv(P, yl + 1, xl + 4), z);
     };
     unsigned seq = 0;
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(kSThreads, 2)
 #pragma unroll
                     for (int u = 0; u < 2; ++u) {
                         const int xl = 2 * lane + u;
-                        const unsigned f = Gv(P, yl, xl + 16);
+                        const unsigned f = Gv(P, yl + 1, xl + 16);
                         const float pc = S[q & 3][yl + 1][xl + 1];
                         const float gy_lo = (f & YLO) ? -sub_rn(pc, S[q & 3][yl][xl + 1]) : 0.f;
                         const float gy_hi = (f & YHI) ? -sub_rn(S[q & 3][yl + 2][xl + 1], pc) : 0.f;

@@ -190,3 +190,25 @@ def test_batch_mg_projection_divergence(pg, oracle):
         vel = B.faces_of(v, i).cpu().numpy().astype(np.float64)
         div = oracle.divergence_rhs(vel, d, fs)
         assert np.abs(div).max() <= 1e-5 * stats[i]["b_max"] + 4e-6 * np.abs(vel).max(), (i, d)
+
+
+def test_batch_mg_long_run_converges(pg):
+    """The 512-grid batch configuration for 12 steps with MG: every grid
+    converges in every step (a single-component grid whose rounding-level
+    inconsistent constant mode used to stall the solve at step 9)."""
+    import torch
+
+    from panopaea_gb300 import workloads as W
+
+    dims, masks, srcs = W.batch_grids(512)
+    B = pg.Batch2d(dims)
+    B.set_solid_cells(masks)
+    v, rho, p = B.new_faces(), B.new_cells(), B.new_cells()
+    src = torch.from_numpy(B.pack_cells(srcs)).cuda()
+    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True,
+                        solver=pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=400))
+    for k in range(12):
+        st = B.step(cfg, v, rho, p, source_field=src)
+        bad = [(i, s["iterations"], s["status"]) for i, s in enumerate(st) if s["status"] != 0 or s["iterations"] > 12]
+        assert not bad, (k, bad[:5])
