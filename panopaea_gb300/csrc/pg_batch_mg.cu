@@ -12,7 +12,8 @@
 // shared memory by symmetric sweeps.  Grids have different depths:
 // level l of the batch packs level l of every grid deep enough, each stage
 // is ONE launch over a tile list of that level (smoothing tiles of 64 x 8
-// cells, two cells of one colour per thread; restriction tiles of 32 x 8
+// cells on level 0, 64 x 32 above, one cell of the colour per row and
+// thread; restriction tiles of 32 x 8
 // coarse cells), and the coarsest solve is one launch with one block per
 // grid, each at its own coarsest level.  Tiles of grids whose CG has
 // converged return at once.  The last fine half-sweep writes one z.r
@@ -27,7 +28,11 @@ namespace pg {
 constexpr int kBmgMaxLevels = 16;
 constexpr int kBmgCoarseMax = 2048;
 constexpr int kBmgCoarseThreads = 512;
-constexpr int kSmTX = 32, kSmTY = 8;  // smoothing tile: 64 x 8 cells, 256 threads
+constexpr int kSmTX = 32, kSmTY = 8;  // smoothing block: 256 threads, 32 x 8
+// rows per thread (kSmTY apart) on level 0 and on the coarser levels: a
+// smoothing tile is 64 x (8 sm_rows) cells
+constexpr int kSmRows0 = 1, kSmRows = 4;
+__host__ __device__ constexpr int sm_rows(bool l0) { return l0 ? kSmRows0 : kSmRows; }
 constexpr int kRtX = 32, kRtY = 8;    // restriction tile: 32 x 8 coarse cells
 
 struct BLevel {
@@ -121,10 +126,58 @@ __device__ __forceinline__ float bnb(const BLv& v, const BLevel& L, i64 k, int y
     return v.e[k];
 }
 
+// What one red-black update of cell c = (y, x) reads, loaded before any of
+// it is used: a neighbour outside the grid is read at the cell itself (the
+// weight of a boundary face is 0, so it is never added), so a thread's
+// loads for all its rows issue together instead of waiting on the flags.
+template <bool L0, int MODE> struct BUpd {
+    float f, inv, w[4], n[4];
+    __device__ __forceinline__ void load(const BLv& v, const BLevel& L, i64 c, int y, int x) {
+        const int h = L.h, wd = L.w;
+        const bool xl = x > 0, xh = x + 1 < wd, yl = y > 0, yh = y + 1 < h;
+        f = v.f[c];
+        if (L0) {
+            const unsigned fl = v.flags[c];
+            w[0] = (fl & XLO) ? v.dt : 0.f;
+            w[1] = (fl & XHI) ? v.dt : 0.f;
+            w[2] = (fl & YLO) ? v.dt : 0.f;
+            w[3] = (fl & YHI) ? v.dt : 0.f;
+            const int nn = __popc(fl);
+            inv = nn ? __frcp_rn((float)nn * v.dt) : 0.f;
+        } else {
+            const float wxh = v.wx[xh ? c + 1 : c], wyh = v.wy[yh ? c + wd : c];
+            w[0] = v.wx[c];
+            w[1] = xh ? wxh : 0.f;
+            w[2] = v.wy[c];
+            w[3] = yh ? wyh : 0.f;
+            inv = v.invd[c];
+        }
+        if (MODE != BNB_SELF) {
+            n[0] = bnb<L0, MODE>(v, L, xl ? c - 1 : c, y, xl ? x - 1 : x);
+            n[1] = bnb<L0, MODE>(v, L, xh ? c + 1 : c, y, xh ? x + 1 : x);
+            n[2] = bnb<L0, MODE>(v, L, yl ? c - wd : c, yl ? y - 1 : y, x);
+            n[3] = bnb<L0, MODE>(v, L, yh ? c + wd : c, yh ? y + 1 : y, x);
+        }
+    }
+    // f + sum over the open faces of weight * neighbour, times 1 / diagonal
+    __device__ __forceinline__ float value() const {
+        float s = f;
+        if (MODE != BNB_SELF) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (w[j] != 0.f) s += w[j] * n[j];
+        }
+        return s * inv;
+    }
+};
+
 // One red-black half-sweep of colour `color` at one level of every grid
-// that smooths there; with RZ (level 0, last) also the per-tile z.r.
+// that smooths there; with RZ (level 0, last) also the per-tile z.r and
+// sum(z).  A thread updates one cell of the colour in each of sm_rows(L0)
+// rows (kSmTY apart): loads of all rows first, then the updates, then
+// the stores.
 template <bool L0, int MODE, bool RZ>
-__global__ void __launch_bounds__(kSmTX * kSmTY)
+__global__ void __launch_bounds__(kSmTX * kSmTY, L0 ? 8 : 3)
     k_bmg_smooth(BLv v, const Tile* __restrict__ tiles, int ntiles, int color, const BState* __restrict__ st,
                  double* __restrict__ partials) {
     __shared__ F2 sm[64];
@@ -135,36 +188,51 @@ __global__ void __launch_bounds__(kSmTX * kSmTY)
         const bool upd = L.coarse > v.level;
         if (!upd && !RZ) continue;
         const int iy = threadIdx.x / kSmTX, ix = threadIdx.x % kSmTX;
-        const int y = t.y0 + iy;
-        const int x = t.x0 + 2 * ix + ((y + color) & 1);
         Acc<float> acc, zs;  // z.r and sum(z) (RZ)
-        if (y < L.h && x < L.w) {
-            const i64 c = L.off + (i64)y * L.w + x;
-            if (upd) {
-                const BCell<L0> cl(v, c, y, x, L.h, L.w);
-                float s = v.f[c];
-                if (MODE == BNB_SELF) {
-                    v.e[c] = s * cl.inv;
-                } else {
-                    if (cl.wxl != 0.f) s += cl.wxl * bnb<L0, MODE>(v, L, c - 1, y, x - 1);
-                    if (cl.wxh != 0.f) s += cl.wxh * bnb<L0, MODE>(v, L, c + 1, y, x + 1);
-                    if (cl.wyl != 0.f) s += cl.wyl * bnb<L0, MODE>(v, L, c - L.w, y - 1, x);
-                    if (cl.wyh != 0.f) s += cl.wyh * bnb<L0, MODE>(v, L, c + L.w, y + 1, x);
-                    v.e[c] = s * cl.inv;
+        constexpr int R = sm_rows(L0);
+        BUpd<L0, MODE> u[R];
+        float ev[R], eo[R], fo[R];  // the colour's new values; the other colour's e, f (RZ)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int y = t.y0 + iy + r * kSmTY;
+            const int x = t.x0 + 2 * ix + ((y + color) & 1);
+            if (y < L.h && x < L.w) {
+                const i64 c = L.off + (i64)y * L.w + x;
+                if (upd) u[r].load(v, L, c, y, x);
+                else if (RZ) {
+                    u[r].f = v.f[c];
+                    ev[r] = v.e[c];
                 }
             }
-            if (RZ) {
-                acc.add(v.e[c] * v.f[c]);
-                zs.add(v.e[c]);
+            // the other colour is not written by this launch: read it now
+            const int xo = t.x0 + 2 * ix + ((y + color + 1) & 1);
+            if (RZ && y < L.h && xo < L.w) {
+                const i64 c = L.off + (i64)y * L.w + xo;
+                eo[r] = v.e[c];
+                fo[r] = v.f[c];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int y = t.y0 + iy + r * kSmTY;
+            const int x = t.x0 + 2 * ix + ((y + color) & 1);
+            if (y < L.h && x < L.w) {
+                if (upd) {
+                    ev[r] = u[r].value();
+                    v.e[L.off + (i64)y * L.w + x] = ev[r];
+                }
+                if (RZ) {
+                    acc.add(ev[r] * u[r].f);
+                    zs.add(ev[r]);
+                }
+            }
+            const int xo = t.x0 + 2 * ix + ((y + color + 1) & 1);
+            if (RZ && y < L.h && xo < L.w) {
+                acc.add(eo[r] * fo[r]);
+                zs.add(eo[r]);
             }
         }
         if (RZ) {
-            const int xo = t.x0 + 2 * ix + ((y + color + 1) & 1);
-            if (y < L.h && xo < L.w) {
-                const i64 c = L.off + (i64)y * L.w + xo;
-                acc.add(v.e[c] * v.f[c]);
-                zs.add(v.e[c]);
-            }
             double a, b;
             tsum2(f2_of(acc), f2_of(zs), sm, &a, &b);
             if (threadIdx.x == 0) {
@@ -186,20 +254,31 @@ __global__ void __launch_bounds__(kRtX * kRtY)
         const BLevel L = v.info[t.grid];
         const int Y = t.y0 + (int)threadIdx.x / kRtX, X = t.x0 + (int)threadIdx.x % kRtX;
         if (Y >= L.ch || X >= L.cw) continue;
-        const int y1 = min(2 * Y + 2, L.h), x1 = min(2 * X + 2, L.w);
-        float sum = 0.f;
-        for (int y = 2 * Y; y < y1; ++y)
-            for (int x = 2 * X; x < x1; ++x) {
+        // the (up to) four children's loads first, then their residuals in
+        // row-major order
+        BUpd<L0, BNB_PLAIN> u[4];
+        float ec[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int y = 2 * Y + (k >> 1), x = 2 * X + (k & 1);
+            if (y < L.h && x < L.w) {
                 const i64 c = L.off + (i64)y * L.w + x;
-                const BCell<L0> cl(v, c, y, x, L.h, L.w);
-                const float ecv = v.e[c];
-                float a = 0.f;
-                if (cl.wxl != 0.f) a += cl.wxl * (ecv - v.e[c - 1]);
-                if (cl.wxh != 0.f) a += cl.wxh * (ecv - v.e[c + 1]);
-                if (cl.wyl != 0.f) a += cl.wyl * (ecv - v.e[c - L.w]);
-                if (cl.wyh != 0.f) a += cl.wyh * (ecv - v.e[c + L.w]);
-                sum += v.f[c] - a;
+                u[k].load(v, L, c, y, x);
+                ec[k] = v.e[c];
             }
+        }
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int y = 2 * Y + (k >> 1), x = 2 * X + (k & 1);
+            if (y < L.h && x < L.w) {
+                float a = 0.f;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (u[k].w[j] != 0.f) a += u[k].w[j] * (ec[k] - u[k].n[j]);
+                sum += u[k].f - a;
+            }
+        }
         fc[L.coff + (i64)Y * L.cw + X] = sum;
     }
 }
@@ -444,7 +523,7 @@ static int bmg_build(pg_batch* B, float dt) {
             BLevel& L = info[l][g];
             if (l == 0) L.t0 = (int)st.size();
             if (l == 0 || l < coarse[g]) {
-                for (int y0 = 0; y0 < L.h; y0 += kSmTY)
+                for (int y0 = 0; y0 < L.h; y0 += kSmTY * sm_rows(l == 0))
                     for (int x0 = 0; x0 < L.w; x0 += 2 * kSmTX) st.push_back(Tile{g, y0, x0});
                 if (l < coarse[g]) M->nsmoothing[l] += 1;
             }
