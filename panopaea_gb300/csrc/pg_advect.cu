@@ -29,15 +29,16 @@ __global__ void k_advect_2d(T* __restrict__ dst, const T* __restrict__ q, const 
 // advect, 3D extension
 template <class T, class I>
 __global__ void k_advect_3d(T* __restrict__ dst, const T* __restrict__ q, const T* __restrict__ vel, Dims D, T ndt,
-                            T hix, T hiy, T hiz) {
+                            T hix, T hiy, T hiz, FastDiv fw, FastDiv fh) {
     const I d = (I)D.d, h = (I)D.h, w = (I)D.w, hw = h * w;
     const I offy = (I)D.offy(), offx = (I)D.offx();
     auto FX = [&](I z, I y, I x) { return offx + (z * h + y) * (w + 1) + x; };
     auto FY = [&](I z, I y, I x) { return offy + (z * (h + 1) + y) * w + x; };
     auto FZ = [&](I z, I y, I x) { return (z * h + y) * w + x; };
     GRID_STRIDE(i, d * hw) {
-        const I zy = i / w, x = i - zy * w;
-        const I z = zy / h, y = zy - z * h;
+        I x, y;
+        const I zy = split(i, w, fw, x);
+        const I z = split(zy, h, fh, y);
         const T vcx = half_rn(add_rn(vel[FX(z, y, x)], vel[FX(z, y, x + 1)]));
         const T vcy = half_rn(add_rn(vel[FY(z, y, x)], vel[FY(z, y + 1, x)]));
         const T vcz = half_rn(add_rn(vel[FZ(z, y, x)], vel[FZ(z + 1, y, x)]));
@@ -93,7 +94,7 @@ __device__ __forceinline__ T sample_part(const T* __restrict__ q, I nz, I ny, I 
 // advect_mac, 3D extension
 template <class T, class I>
 __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, Dims D,
-                                T ndt) {
+                                T ndt, FastDiv fexy, FastDiv fex) {
     const I d = (I)D.d, h = (I)D.h, w = (I)D.w;
     const I nz = (I)D.nfz(), ny = (I)D.nfy();
     auto FX = [&](I z, I y, I x) { return nz + ny + (z * h + y) * (w + 1) + x; };
@@ -108,8 +109,9 @@ __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, 
     // parts one after another re-reads each part from DRAM).
     const I ex = w + 1, exy = (h + 1) * ex;
     GRID_STRIDE(t, (d + 1) * exy) {
-        const I z = t / exy, r = t - z * exy;
-        const I y = r / ex, x = r - y * ex;
+        I r, x;
+        const I z = split(t, exy, fexy, r);
+        const I y = split(r, ex, fex, x);
         if (z < d && y < h) {  // x face (z, y, x), part dims (d, h, w+1)
             const I i = FX(z, y, x);
             const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
@@ -153,12 +155,16 @@ template <class T> int launch_advect(const pg_grid* g, T* dst, const T* src, dou
         if (D.nd == 2)
             PG_LAUNCH(KK_ADVECT, s, k_advect_2d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, (int)D.h, (int)D.w, ndt, hix, hiy));
         else
-            PG_LAUNCH(KK_ADVECT, s, k_advect_3d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, hix, hiy, hiz));
+            PG_LAUNCH(KK_ADVECT, s,
+                      k_advect_3d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, hix, hiy, hiz,
+                                                                  fast_div((unsigned)D.w), fast_div((unsigned)D.h)));
     } else {
         if (D.nd == 2)
             PG_LAUNCH(KK_ADVECT, s, k_advect_2d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D.h, D.w, ndt, hix, hiy));
         else
-            PG_LAUNCH(KK_ADVECT, s, k_advect_3d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, hix, hiy, hiz));
+            PG_LAUNCH(KK_ADVECT, s,
+                      k_advect_3d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, hix, hiy, hiz, FastDiv{},
+                                                                  FastDiv{}));
     }
     PG_CHECK_LAUNCH();
     return PG_OK;
@@ -173,12 +179,15 @@ template <class T> int launch_advect_mac(const pg_grid* g, T* dst, const T* src,
         if (D.nd == 2)
             PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_2d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, (int)D.h, (int)D.w, ndt));
         else
-            PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_3d<T, int><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt));
+            PG_LAUNCH(KK_ADVECT_MAC, s,
+                      k_advect_mac_3d<T, int><<<nb, kThreads, 0, s>>>(
+                          dst, src, vel, D, ndt, fast_div((unsigned)((D.h + 1) * (D.w + 1))), fast_div((unsigned)(D.w + 1))));
     } else {
         if (D.nd == 2)
             PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_2d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D.h, D.w, ndt));
         else
-            PG_LAUNCH(KK_ADVECT_MAC, s, k_advect_mac_3d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt));
+            PG_LAUNCH(KK_ADVECT_MAC, s,
+                      k_advect_mac_3d<T, i64><<<nb, kThreads, 0, s>>>(dst, src, vel, D, ndt, FastDiv{}, FastDiv{}));
     }
     PG_CHECK_LAUNCH();
     return PG_OK;

@@ -101,11 +101,12 @@ __global__ void k_laplacian(T* __restrict__ out, const T* __restrict__ p, const 
 // reference never masks them, and then face_solid is NULL).
 template <class T, int ND, class I>
 __global__ void k_rhs(T* __restrict__ b, const T* __restrict__ vel, const uint8_t* __restrict__ flags,
-                      const uint8_t* __restrict__ fsolid, Dims D) {
+                      const uint8_t* __restrict__ fsolid, Dims D, FastDiv fw, FastDiv fh) {
     const I h = D.h, w = D.w;
     GRID_STRIDE_I(c, (I)D.nc()) {
-        const I zy = c / w, x = c - zy * w;
-        const I z = zy / h, y = zy - z * h;
+        I x, y;
+        const I zy = split(c, w, fw, x);
+        const I z = split(zy, h, fh, y);
         const uint8_t f = flags[c];
         // Is a face masked?  Interior faces: the cell's open bit; boundary
         // faces: the per-face solid array (NULL = never masked).
@@ -258,9 +259,9 @@ template <class T> int launch_laplacian(const pg_grid* g, T* out, const T* p, do
 template <class T> int launch_rhs(const pg_grid* g, T* b, const T* vel) {
     const Dims& D = g->dims;
     if (D.nd == 2)
-        PG_IDX(g, PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 2, I><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D)));
+        PG_IDX(g, PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 2, I><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D, fast_div_for<I>(D.w), fast_div_for<I>(D.h))));
     else
-        PG_IDX(g, PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 3, I><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D)));
+        PG_IDX(g, PG_LAUNCH(KK_RHS, g->stream, k_rhs<T, 3, I><<<grid_blocks(g, D.nc(), kThreads), kThreads, 0, g->stream>>>(b, vel, g->flags, g->face_solid, D, fast_div_for<I>(D.w), fast_div_for<I>(D.h))));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }
@@ -291,31 +292,42 @@ __device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl)
     return __fadd_rn(s, __fadd_rn(e, __fsub_rn(al, bl)));
 }
 
+// Divisors of the face index split: h w, w, h + 1, w + 1.
+struct FaceDivs {
+    FastDiv hw, w, h1, w1;
+};
+template <class I> inline FaceDivs face_divs(const Dims& D) {
+    return FaceDivs{fast_div_for<I>(D.h * D.w), fast_div_for<I>(D.w), fast_div_for<I>(D.h + 1), fast_div_for<I>(D.w + 1)};
+}
+
 template <class I>
 __global__ void k_project_df(float* vel, const float* src, const float* __restrict__ ph, const float* __restrict__ pl,
-                             const uint8_t* __restrict__ flags, Dims D, float dt, int zero_solid) {
+                             const uint8_t* __restrict__ flags, Dims D, float dt, int zero_solid, FaceDivs fd) {
     const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
     const I h = (I)D.h, w = (I)D.w, hw = h * w, d = (I)D.d;
     GRID_STRIDE_I(i, nf) {
         I lo, hi;
         uint8_t bit;
         if (i < nz) {
-            const I z = i / hw, r = i - z * hw;
+            I r;
+            const I z = split(i, hw, fd.hw, r);
             if (z == 0 || z == d) { vel[i] = 0.f; continue; }
             hi = z * hw + r;
             lo = hi - hw;
             bit = ZLO;
         } else if (i < nz + ny) {
             const I j = i - nz;
-            const I zy = j / w, x = j - zy * w;
-            const I z = zy / (h + 1), y = zy - z * (h + 1);
+            I x, y;
+            const I zy = split(j, w, fd.w, x);
+            const I z = split(zy, h + 1, fd.h1, y);
             if (y == 0 || y == h) { vel[i] = 0.f; continue; }
             hi = (z * h + y) * w + x;
             lo = hi - w;
             bit = YLO;
         } else {
             const I j = i - nz - ny;
-            const I zy = j / (w + 1), x = j - zy * (w + 1);
+            I x;
+            const I zy = split(j, w + 1, fd.w1, x);
             if (x == 0 || x == w) { vel[i] = 0.f; continue; }
             hi = zy * w + x;
             lo = hi - 1;
@@ -332,7 +344,7 @@ int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float
     const Dims& D = g->dims;
     PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream,
               k_project_df<I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
-                  vel, src ? src : vel, ph, pl, g->flags, D, (float)dt, zero_solid)));
+                  vel, src ? src : vel, ph, pl, g->flags, D, (float)dt, zero_solid, face_divs<I>(D))));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }

@@ -53,6 +53,39 @@ __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(
 template <class T> __device__ __forceinline__ T half_rn(T x) { return mul_rn(x, T(0.5)); }
 template <class T> __device__ __forceinline__ T quarter_rn(T x) { return mul_rn(x, T(0.25)); }
 
+// Index splitting by a divisor fixed for the launch: the quotient of a 32-bit
+// n by d >= 2 with one multiply-high instead of an integer division sequence
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", 1994, the round-up method): l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1, t = umulhi(m, n),
+// n / d = (t + ((n - t) >> 1)) >> (l - 1), exact for every 32-bit n.
+// m >= 1 for every d >= 2; m = 0 stands for d = 1.
+struct FastDiv {
+    unsigned m = 0, s = 0;
+};
+inline FastDiv fast_div(unsigned d) {
+    FastDiv f;
+    if (d < 2) return f;
+    unsigned l = 0;
+    while ((1ull << l) < d) ++l;
+    f.m = (unsigned)((((unsigned long long)1 << 32) * ((1ull << l) - d)) / d + 1);
+    f.s = l - 1;
+    return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned n, FastDiv f) {
+    const unsigned t = __umulhi(n, f.m);
+    return f.m ? (t + ((n - t) >> 1)) >> f.s : n;
+}
+// (i / d, i % d) of a flat index; fd = fast_div(d), used when I is 32-bit
+// (indices below 2^31).
+template <class I> __device__ __forceinline__ I split(I i, I d, FastDiv fd, I& rem) {
+    const I q = sizeof(I) == 4 ? (I)fdiv((unsigned)i, fd) : i / d;
+    rem = i - q * d;
+    return q;
+}
+// fast_div for a launch whose index type is I (nothing to do for 64-bit).
+template <class I> inline FastDiv fast_div_for(i64 d) { return sizeof(I) == 4 ? fast_div((unsigned)d) : FastDiv{}; }
+
 // math/interp.rs:7-12: a0*(1-s) + a1*s
 template <class T> __device__ __forceinline__ T lerp_ref(T a0, T a1, T s) {
     return add_rn(mul_rn(a0, sub_rn(T(1), s)), mul_rn(a1, s));

@@ -28,7 +28,9 @@ template <class T, class I> __device__ __forceinline__ void face_coord(T pos, T 
     const T p = fmax(floor(q), T(0));
     const T last = (T)(n - 1);
     i0 = (I)fmin(p, last);
-    i1 = (I)fmin(add_rn(p, T(1)), last);
+    // = (I)fmin(p + 1, last): p is integer-valued, so either p >= last
+    // (both give n - 1) or p <= n - 2 and p + 1 is exact
+    i1 = i0 + 1 < n ? i0 + 1 : n - 1;
     // .min(1.0).max(0.0) with Rust's NaN rule: NaN.min(1) = 1.  Written out
     // because the compiler turns fmax(fmin(v, 1), 0) into a saturate, which
     // maps NaN to 0.
