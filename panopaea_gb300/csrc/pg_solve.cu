@@ -125,6 +125,12 @@ __global__ void k_x64_add(double* __restrict__ x, const float* __restrict__ d, i
         x[c] += (double)d[c];
 }
 
+// x = 0 + d: k_x64_add onto a zeroed x without reading (or zeroing) it.
+__global__ void k_x64_set(double* __restrict__ x, const float* __restrict__ d, i64 n) {
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x)
+        x[c] = 0.0 + (double)d[c];
+}
+
 __global__ void k_x64_store(float* __restrict__ out, const double* __restrict__ x, i64 n) {
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x)
         out[c] = (float)x[c];
@@ -311,6 +317,19 @@ __global__ void k_xdf_add(float* __restrict__ xh, float* __restrict__ xl, const 
     }
 }
 
+// x = 0 + d: the arithmetic of k_xdf_add with xh = xl = 0, without reading
+// (or zeroing) them -- the same bits for every d, -0 and NaN included.
+__global__ void k_xdf_set(float* __restrict__ xh, float* __restrict__ xl, const float* __restrict__ d, i64 n) {
+    for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x) {
+        float s, e;
+        two_sum(0.f, d[c], s, e);
+        const float lo = __fadd_rn(0.f, e);
+        const float h2 = __fadd_rn(s, lo);
+        xh[c] = h2;
+        xl[c] = __fsub_rn(lo, __fsub_rn(h2, s));
+    }
+}
+
 __global__ void k_xdf_store(float* __restrict__ out, const float* __restrict__ xh, const float* __restrict__ xl, i64 n) {
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (i64)gridDim.x * blockDim.x)
         out[c] = __fadd_rn(xh[c], xl[c]);
@@ -401,7 +420,6 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
         return rc;
     void* rin;
     if ((rc = ex->buffer(Extras::kRin, 4 * n, &rin))) return rc;
-    PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
     const int nb = grid_blocks(g, n, kThreads, 8);
     const bool native = prm->fp64_native != 0;
     float* xh = (float*)x64;
@@ -413,6 +431,12 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     int rounds = 0;
     const bool guess = prm->initial_guess != 0;
     bool done = false;
+    // x = 0: zeroed here only when a guess is added to it; otherwise the
+    // first round's correction is stored into it (k_*_set), and a solve
+    // that ends before storing any (b = 0, NaN, breakdown) zeroes it at the
+    // end.
+    bool x_set = guess;
+    if (guess) PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
     if (guess) {
         // ||b||inf from the residual of x = 0, then the residual of the guess.
         if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &bmax))) return rc;
@@ -480,11 +504,18 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
             out.status = s.status;
             break;
         }
-        if (native)
+        if (from_b) {  // x was 0: x = d
+            if (native)
+                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_set<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
+            else
+                PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_set<<<nb, kThreads, 0, g->stream>>>(xh, xl, (const float*)d, n));
+        } else if (native) {
             PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_add<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
-        else
+        } else {
             PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_add<<<nb, kThreads, 0, g->stream>>>(xh, xl, (const float*)d, n));
+        }
         PG_CHECK_LAUNCH();
+        x_set = true;
         if ((rc = residual64(g, b, x64, native, dt, (float*)rin, &rmax))) return rc;
         if (!std::isfinite(rmax)) {
             out.status = PG_NAN_DETECTED;
@@ -498,6 +529,7 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     }
     out.b_max = bmax;
     out.threshold = target;
+    if (!x_set) PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
     if (native)
         PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n));
     else
