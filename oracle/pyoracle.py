@@ -1,7 +1,8 @@
 """numpy front-end of the C++ oracle (test infrastructure only).
 
 Only the test-suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
-baseline use this module, always as the checker / the timed CPU reference;
+baseline use this module, always as the results to compare against or the
+timed CPU baseline;
 the product (``panopaea_gb300``) never imports it.
 
 Arrays follow the reference layouts: 2D cells (h, w), faces
