@@ -66,7 +66,9 @@ BYTES_PER_CELL = {
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 50: a timed region long enough for the clock samples to fall in; "
+                         "5 bounded CPU samples for --impl reference)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="precision_3d_256")
@@ -81,7 +83,10 @@ def parse_args():
     ap.add_argument("--held", type=int, default=32, help="learned_3d_128: held-out grids")
     ap.add_argument("--gen", default="mg", choices=["mg", "plain"], help="learned_3d_128: solver of the pairs")
     ap.add_argument("--batch-count", type=int, default=512, help="batch_512: number of grids")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.impl == "reference" else 50
+    return args
 
 
 # ---------------------------------------------------------------------------
@@ -147,14 +152,18 @@ class Clocks:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # the timed region starts once the sampler is producing samples
+            t_end = time.time() + 3.0
+            while time.time() < t_end and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
 
     def stop(self):
         if not self.proc:
             return None
-        time.sleep(0.25)
+        time.sleep(0.06)  # the sample in flight at the end of the region
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
