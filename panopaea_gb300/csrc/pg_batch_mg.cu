@@ -13,9 +13,8 @@
 // level l of the batch packs level l of every grid deep enough, each stage
 // is ONE launch over a tile list of that level (smoothing tiles of 64 x 8
 // cells on level 0, 64 x 32 above, one cell of the colour per row and
-// thread; restriction tiles of 32 x 8
-// coarse cells), and the coarsest solve is one launch with one block per
-// grid, each at its own coarsest level.  Tiles of grids whose CG has
+// thread; restriction tiles of 32 x 8 coarse cells), and the coarsest solve
+// is one launch with one block per grid, each at its own coarsest level.  Tiles of grids whose CG has
 // converged return at once.  The last fine half-sweep writes one z.r
 // partial per tile; a per-grid block folds them in a fixed order.
 #include <algorithm>
