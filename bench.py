@@ -169,8 +169,19 @@ class Clocks:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        with open(self.path) as f:
+            lines = f.read().splitlines()
+        os.unlink(self.path)
+        return self.summarize(lines)
+
+    @staticmethod
+    def summarize(lines):
+        """nvidia-smi CSV rows (the query Q, no header, no units) -> the
+        `clocks` object: median SM clock over the loaded samples (power at
+        least half the peak seen), the maximum clock, and every throttle
+        reason that was active in any sample."""
         rows = []
-        for ln in open(self.path):
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -179,7 +190,6 @@ class Clocks:
                                  pcap=f[8]))
             except ValueError:
                 continue
-        os.unlink(self.path)
         if not rows:
             return None
         pmax = max(r["power"] for r in rows)
