@@ -15,6 +15,10 @@ Two solver forms run on the same workload:
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+K defaults to 50 (0.24 s of timed work at 256^3, so the clock samples --
+nvidia-smi polled every 50 ms from before the timed region -- fall inside
+it), W to 3; the reference arm defaults to 5 bounded CPU samples.
+
 Multi-GPU (torchrun, one rank per GPU): every rank advances its own replica
 grid (the step has no data-path exchange), `value` = all cells x steps over
 the max time over ranks ("scaling": "weak").
