@@ -16,6 +16,7 @@
 // each thread accumulates a compensated FP32 partial (float fields) and
 // only the cross-thread and cross-block reduction tree is FP64.
 #include <algorithm>
+#include <cstdlib>
 
 #include "pg_cg.cuh"
 
@@ -301,14 +302,16 @@ __global__ void __launch_bounds__(kTX * kTY)
     }
 }
 
-// Launch the fused SpMV: the 2.5D tile for 3D grids, the flat grid-stride
-// kernel for 2D.  Shared by every CG entry point.
+// Launch the fused SpMV: the TMA-staged z-marching kernel for 3D float grids
+// where it applies (tma = true), else the 2.5D tile for 3D grids and the
+// flat grid-stride kernel for 2D.  Shared by every CG entry point.
 template <class T, int PM>
 static void spmv_launch(cudaStream_t s, int num_sms, const T* r, const T* zb, T* p0, T* p1, T* ap,
-                        const uint8_t* flags, const Dims& D, T dt, CgState* st, double* partials, int nb_flat) {
-    if (PM == PM_ZBUF && sizeof(T) == 4 &&
-        spmv_tma_launch(s, num_sms, (const float*)zb, (float*)p0, (float*)p1, (float*)ap, flags, D, (float)dt, st,
-                        partials))
+                        const uint8_t* flags, const Dims& D, T dt, CgState* st, double* partials, int nb_flat,
+                        bool tma = true) {
+    if (tma && sizeof(T) == 4 &&
+        spmv_tma_launch(s, num_sms, PM, (const float*)(PM == PM_ZBUF ? zb : r), (float*)p0, (float*)p1, (float*)ap,
+                        flags, D, (float)dt, st, partials))
         return;
     if (D.nd == 3) {
         const int tiles_x = (int)((D.w + kTX - 1) / kTX), tiles_y = (int)((D.h + kTY - 1) / kTY);
@@ -443,6 +446,94 @@ __global__ void __launch_bounds__(kCgThreads)
     }
 }
 
+// The update of the identity / Jacobi CG on float4 vectors, two per thread
+// and iteration (eight cells' x, p, r, Ap in flight per thread): the same
+// per-cell arithmetic as k_cg_update<float, PM> and the same compensated
+// FP32 partial of z.r per thread (summed in a different order); Jacobi reads
+// the cells' face-open bits four at a time.  n4 = n / 4.
+template <int PM>
+__global__ void __launch_bounds__(kCgThreads)
+    k_cg_update4r(float4* __restrict__ x, float4* __restrict__ r, const float4* p0, const float4* p1,
+                  const float4* __restrict__ ap, const uchar4* __restrict__ flags, i64 n4, float dt, CgState* st,
+                  double* partials) {
+    if (st->done) return;
+    __shared__ double sm[32];
+    __shared__ float inv_diag[8];  // Jacobi: 1 / (n dt) for n open faces (0 for n = 0), as zof computes it
+    if (PM == PM_JACOBI) {
+        if (threadIdx.x < 8) inv_diag[threadIdx.x] = threadIdx.x ? __frcp_rn((float)threadIdx.x * dt) : 0.f;
+        __syncthreads();
+    }
+    const i64 k = *(volatile const i64*)&st->iter;
+    const float4* __restrict__ p = ((k + 1) & 1) ? p1 : p0;
+    const float alpha = (float)st->alpha, nalpha = -alpha;
+    float rm = 0.f;
+    Acc<float> rz;
+    int bad = 0;
+    auto zr = [&](float rv, unsigned f) {
+        if (PM == PM_JACOBI) {
+            const float z = f ? rv * inv_diag[__popc(f)] : 0.f;
+            rz.add(z * rv);
+        } else {
+            rz.add(rv * rv);
+        }
+    };
+    auto one = [&](i64 c) {
+        const float4 xv = x[c], pv = p[c], rv = r[c], av = ap[c];
+        uchar4 f = make_uchar4(0, 0, 0, 0);
+        if (PM == PM_JACOBI) f = flags[c];
+        float4 xo, ro;
+        xo.x = xv.x + alpha * pv.x;  // pcg.rs:55
+        xo.y = xv.y + alpha * pv.y;
+        xo.z = xv.z + alpha * pv.z;
+        xo.w = xv.w + alpha * pv.w;
+        ro.x = rv.x + nalpha * av.x;  // pcg.rs:56
+        ro.y = rv.y + nalpha * av.y;
+        ro.z = rv.z + nalpha * av.z;
+        ro.w = rv.w + nalpha * av.w;
+        x[c] = xo;
+        r[c] = ro;
+        rm = fmaxf(fmaxf(fmaxf(rm, fabsf(ro.x)), fmaxf(fabsf(ro.y), fabsf(ro.z))), fabsf(ro.w));
+        bad |= !isfinite(ro.x) | !isfinite(ro.y) | !isfinite(ro.z) | !isfinite(ro.w);
+        zr(ro.x, f.x);
+        zr(ro.y, f.y);
+        zr(ro.z, f.z);
+        zr(ro.w, f.w);
+    };
+    const i64 stride = (i64)gridDim.x * blockDim.x;
+    i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; c + stride < n4; c += 2 * stride) {
+        one(c);
+        one(c + stride);
+    }
+    if (c < n4) one(c);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->nan_seen, 1);
+    const double m = block_max<kCgThreads>((double)rm, sm);
+    const double s = block_sum<kCgThreads>(rz.value(), sm);
+    if (threadIdx.x == 0) {
+        partials[2 * kMaxBlocks + blockIdx.x] = m;
+        partials[3 * kMaxBlocks + blockIdx.x] = s;
+    }
+    if (!last_block(&st->counter[2])) return;
+    const double rmax = reduce_partials<true, kCgThreads>(partials + 2 * kMaxBlocks, gridDim.x, sm);
+    const double sigma_new = reduce_partials<false, kCgThreads>(partials + 3 * kMaxBlocks, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+        st->counter[2] = 0;
+        const i64 it = st->iter + 1;
+        st->iter = it;
+        st->rmax = rmax;
+        if (st->nan_seen || !isfinite(rmax)) {
+            st->status = PG_NAN_DETECTED;
+            st->done = 1;
+        } else if ((float)rmax < (float)st->threshold) {  // pcg.rs:58-63
+            st->status = PG_OK;
+            st->done = 1;
+        } else {
+            cg_finish_rz(st, sigma_new);            // pcg.rs:65-68
+            if (it >= st->max_iter) st->done = 1;  // loop bound, pcg.rs:48
+        }
+    }
+}
+
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 // After max_iterations the reference has already run aux = M r and
@@ -459,20 +550,35 @@ __global__ void k_cg_tail(const T* __restrict__ r, const T* __restrict__ p, T* _
     }
 }
 
+// The identity / Jacobi CG takes the TMA-staged SpMV unless PG_CG_TMA=0 (a
+// diagnostic switch, read per launch sequence: a grid's cached CG graphs keep
+// the choice they were captured with).
+static bool cg_tma_enabled() {
+    const char* env = getenv("PG_CG_TMA");
+    return !(env && env[0] == '0');
+}
+
 template <class T, int PM>
 static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* hook) {
     const Dims& D = g->dims;
     cudaStream_t s = g->stream;
     PG_LAUNCH(KK_CG_SPMV, s,
               spmv_launch<T, PM>(s, g->num_sms, buf.r, buf.z, buf.p[0], buf.p[1], buf.ap, g->flags, D, dt,
-                                 g->ws.state, g->ws.partials, nb));
+                                 g->ws.state, g->ws.partials, nb, PM == PM_ZBUF || cg_tma_enabled()));
     const i64 n = D.nc();
-    if (PM == PM_ZBUF && sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.r) &&
-        aligned16(buf.p[0]) && aligned16(buf.p[1]) && aligned16(buf.ap))
+    const bool vec4 = sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.r) &&
+                      aligned16(buf.p[0]) && aligned16(buf.p[1]) && aligned16(buf.ap) && aligned16(g->flags);
+    if (PM == PM_ZBUF && vec4)
         PG_LAUNCH(KK_CG_UPDATE, s,
                   k_cg_update4<<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.p[0],
                                                          (const float4*)buf.p[1], (const float4*)buf.ap, n / 4,
                                                          g->ws.state, g->ws.partials));
+    else if (PM != PM_ZBUF && vec4)
+        PG_LAUNCH(KK_CG_UPDATE, s,
+                  k_cg_update4r<PM><<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r,
+                                                              (const float4*)buf.p[0], (const float4*)buf.p[1],
+                                                              (const float4*)buf.ap, (const uchar4*)g->flags, n / 4,
+                                                              (float)dt, g->ws.state, g->ws.partials));
     else
         PG_LAUNCH(KK_CG_UPDATE, s,
                   k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, n,
@@ -809,7 +915,8 @@ static int run(const Dims& D, const uint8_t* flags, float* x, const float* b, i6
     while (!done && done_launch < max_iter) {
         const i64 todo = std::min<i64>(chunk, max_iter - done_launch);
         for (i64 k = 0; k < todo; ++k) {
-            spmv_launch<float, PM>(s, sms, residual, nullptr, p[0], p[1], auxiliary, flags, D, fdt, st, partials, nb);
+            spmv_launch<float, PM>(s, sms, residual, nullptr, p[0], p[1], auxiliary, flags, D, fdt, st, partials, nb,
+                                   false);
             k_cg_update<float, PM><<<nb, kCgThreads, 0, s>>>(x, residual, p[0], p[1], auxiliary, flags, n, fdt, st,
                                                              partials);
         }

@@ -49,10 +49,11 @@ template <> struct Acc<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
-// The fused SpMV of the MG path on 3D float grids, TMA-staged (pg_spmv.cu);
-// false when it does not apply (2D, rows not a multiple of 16 cells, a
-// vector that cannot be mapped) and nothing was launched.
-bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, float* p1, float* ap,
+// The fused SpMV on 3D float grids, TMA-staged (pg_spmv.cu), for the
+// preconditioner mode pm (PrecMode): src is z (PM_ZBUF) or r (PM_NONE,
+// PM_JACOBI).  False when it does not apply (2D, rows not a multiple of 16
+// cells, a vector that cannot be mapped) and nothing was launched.
+bool spmv_tma_launch(cudaStream_t s, int num_sms, int pm, const float* src, float* p0, float* p1, float* ap,
                      const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials);
 
 // The double-float residual r = b - A (xh + xl) and ||r||inf (to *out) of the

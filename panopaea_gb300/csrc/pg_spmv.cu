@@ -1,18 +1,21 @@
 // pg_spmv.cu -- TMA-staged z-marching kernels of the 3D solve: the fused
-// SpMV of the multigrid-preconditioned CG (p = z + beta p, Ap, p.Ap;
-// pcg.rs:52-53, 77 with the masked Laplacian of grid.rs) and the
+// SpMV of the CG (p = z + beta p, Ap, p.Ap; pcg.rs:52-53, 77 with the
+// masked Laplacian of grid.rs) for every preconditioner, and the
 // double-float residual b - A x of the refinement.
 //
 // A block owns a kSX x kSY column tile and walks a chunk of z planes.  TMA
-// stages every plane of z and p_old (one-cell halo) and of the face flags
-// (tile only) into a kSStages-deep shared-memory ring; for plane q+1 the
-// block computes p_new = z + beta p_old on the tile and its one-cell ring
-// into a 4-slot plane ring (and stores the tile's values), then A p_new of
-// plane q from the slots of planes q-1, q and q+1.  A staged plane is free
-// as soon as its p_new and its flags have been used, so most of the ring is
-// in flight.  Per cell: 4 bytes of z, 4 of p_old, 1 of flags in; 4 of p_new
-// and 4 of Ap out.  Same per-cell arithmetic as k_cg_spmv3t<float, PM_ZBUF>
-// (the p.Ap reduction runs in a different order).
+// stages every plane of the source vector and p_old (one-cell halo) and of
+// the face flags (tile and halo) into a kSStages-deep shared-memory ring; for
+// plane q+1 the block computes p_new = z + beta p_old on the tile and its
+// one-cell ring into a 4-slot plane ring (and stores the tile's values), then
+// A p_new of plane q from the slots of planes q-1, q and q+1.  A staged plane
+// is free as soon as its p_new and its flags have been used, so most of the
+// ring is in flight.  Per cell: 4 bytes of the source, 4 of p_old, 1 of flags
+// in; 4 of p_new and 4 of Ap out.  The source is z itself (multigrid writes
+// it), or r with z = r (identity, pcg.rs:8-12) or z = r / diag computed from
+// the staged flags once per cell and plane (Jacobi).  Same per-cell
+// arithmetic as k_cg_spmv3t<float, PM> (the p.Ap reduction runs in a
+// different order).
 #include <mutex>
 
 #include "pg_cg.cuh"
@@ -48,6 +51,7 @@ struct SpmvArgs {
     int tiles_x, tiles_y, zc, nwork;
 };
 
+template <int PM>
 __global__ void __launch_bounds__(kSThreads, 2)
     k_cg_spmv3p(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap pmap0,
                 const __grid_constant__ CUtensorMap pmap1, const __grid_constant__ CUtensorMap gmap, SpmvArgs a,
@@ -64,6 +68,9 @@ __global__ void __launch_bounds__(kSThreads, 2)
     float* const p_new = (kit & 1) ? a.p0 : a.p1;
     const int first = st->first;
     const float beta = first ? 0.f : (float)st->beta;
+    // Jacobi: 1 / (n dt) for n open faces, computed as in zval (0 for n = 0)
+    __shared__ float inv_diag[8];
+    if (PM == PM_JACOBI && tid < 8) inv_diag[tid] = tid ? __frcp_rn((float)tid * a.dt) : 0.f;
     if (tid == 0) {
         for (int s = 0; s < kSStages; ++s) mbar_init(&bars[s], 1);
         mbar_fence_init();
@@ -97,10 +104,16 @@ __global__ void __launch_bounds__(kSThreads, 2)
     };
     // p_new of cell (yl, xl) of the staged plane P (tile coordinates), with
     // z projected lazily on the fluid cells (zm = 0 when off)
-    const float zm = st->nfluid > 0.0 ? (float)st->zmean : 0.f;
+    const float zm = (PM == PM_ZBUF && st->nfluid > 0.0) ? (float)st->zmean : 0.f;
     auto pn = [&](const unsigned char* P, int yl, int xl) -> float {
         const float z0 = Zv(P, yl + 1, xl + 4);
-        const float z = Gv(P, yl + 1, xl + 16) ? z0 - zm : z0;
+        float z = z0;
+        if (PM == PM_ZBUF) {
+            z = Gv(P, yl + 1, xl + 16) ? z0 - zm : z0;
+        } else if (PM == PM_JACOBI) {
+            const unsigned f = Gv(P, yl + 1, xl + 16);
+            z = f ? z0 * inv_diag[__popc(f)] : 0.f;
+        }
         return first ? z : fmaf(beta, Pv(P, yl + 1, xl + 4), z);
     };
     unsigned seq = 0;
@@ -429,21 +442,29 @@ bool cached_map(const void* p, int elem, const Dims& D, int bx, int by, CUtensor
     return true;
 }
 
-}  // namespace
-
-bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, float* p1, float* ap,
-                     const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials) {
+template <int PM> static int spmv_cap(int num_sms) {
     static int cap = -1;
     if (cap < 0) {
         cap = 0;
-        if (cudaFuncSetAttribute(k_cg_spmv3p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSSmem) ==
+        if (cudaFuncSetAttribute(k_cg_spmv3p<PM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSSmem) ==
             cudaSuccess) {
             int bps = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cg_spmv3p, kSThreads, kSSmem) == cudaSuccess)
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cg_spmv3p<PM>, kSThreads, kSSmem) ==
+                cudaSuccess)
                 cap = std::min(bps * num_sms, kMaxBlocks);
         }
         cudaGetLastError();
     }
+    return cap;
+}
+
+}  // namespace
+
+bool spmv_tma_launch(cudaStream_t s, int num_sms, int pm, const float* zb, float* p0, float* p1, float* ap,
+                     const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials) {
+    if (pm != PM_NONE && pm != PM_JACOBI && pm != PM_ZBUF) return false;
+    const int cap = pm == PM_ZBUF ? spmv_cap<PM_ZBUF>(num_sms)
+                                  : (pm == PM_JACOBI ? spmv_cap<PM_JACOBI>(num_sms) : spmv_cap<PM_NONE>(num_sms));
     if (cap <= 0 || D.nd != 3 || D.w % 16 != 0 || D.nc() >= ((i64)1 << 31)) return false;
     if (((uintptr_t)ap & 7) || ((uintptr_t)p0 & 7) || ((uintptr_t)p1 & 7)) return false;
     CUtensorMap zm, pm0, pm1, gm;
@@ -465,7 +486,12 @@ bool spmv_tma_launch(cudaStream_t s, int num_sms, const float* zb, float* p0, fl
     a.zc = (a.d + nch - 1) / nch;
     a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
     const int nb = std::max(1, std::min(a.nwork, cap));
-    k_cg_spmv3p<<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
+    if (pm == PM_ZBUF)
+        k_cg_spmv3p<PM_ZBUF><<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
+    else if (pm == PM_JACOBI)
+        k_cg_spmv3p<PM_JACOBI><<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
+    else
+        k_cg_spmv3p<PM_NONE><<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
     return true;
 }
 

@@ -175,3 +175,41 @@ def test_refined_solve_reaches_fp64_tolerance(pg, oracle, dims):
     # x is returned in FP32: allow its rounding on top of the FP64 target
     assert st["true_residual_max"] <= 1e-6 * np.abs(bh).max()
     assert true_r <= 1e-5 * np.abs(bh).max()
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+@pytest.mark.parametrize("dims,obstacle", [((20, 24, 80), True), ((37, 19, 48), False), ((64, 64, 64), True)])
+def test_tma_spmv_equals_tile_kernel(pg, oracle, dims, obstacle, precond, monkeypatch):
+    """The identity / Jacobi CG on 3D grids whose rows are a multiple of 16
+    cells runs the TMA-staged z-marching SpMV and the float4 update; with
+    PG_CG_TMA=0 it runs the 2.5D tile SpMV and the scalar update.  Per-cell
+    arithmetic is the same and only the order of the FP64-class reductions
+    differs, so both give the same iteration count (+-1) and the same
+    solution to 1e-5 of max|x| -- on ragged tiles, with an obstacle."""
+    r = rng(seed_of(dims, obstacle, precond))
+    nf = oracle.num_faces(dims)
+    vel = oracle.walls(r.standard_normal(nf).astype(np.float32), dims)
+    cs = None
+    if obstacle:
+        idx = np.indices(dims).astype(np.float64)
+        ctr = np.array([(n - 1) / 2 for n in dims]).reshape((-1, 1, 1, 1))
+        cs = (((idx - ctr) ** 2).sum(0) < (min(dims) / 4.0) ** 2).astype(np.uint8)
+    res = {}
+    for tma in ("1", "0"):
+        monkeypatch.setenv("PG_CG_TMA", tma)
+        g = make_grid(pg, dims)  # a new grid: no CG graph cached under the other setting
+        if cs is not None:
+            g.set_solid_cells(cs)
+        b = g.new_simplex_2()
+        g.divergence_rhs(b, faces(pg, g, vel))
+        x = g.new_simplex_2()
+        st = pg.solve_pressure(g, x, b, 0.5, pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=1e-5,
+                                                             max_iter=20000))
+        assert st["status"] == 0, (tma, st)
+        res[tma] = (st, host(x).astype(np.float64), host(b).astype(np.float64))
+    (s1, x1, b1), (s0, x0, _) = res["1"], res["0"]
+    assert abs(s1["iterations"] - s0["iterations"]) <= 1, (s1, s0)
+    assert np.abs(x1 - x0).max() <= 1e-5 * np.abs(x0).max()
+    fs = oracle.cell_mask_to_faces(cs) if obstacle else None
+    true_r = np.abs(b1 - oracle.laplacian(x1, 0.5, dims, fs)).max()
+    assert true_r <= 20e-5 * np.abs(b1).max()
