@@ -408,26 +408,69 @@ void apply_laplacian(T* out, const T* p, T dt, const uint8_t* fs, const Shape& s
     }
 }
 
+// Parallel reductions of the all-loops mode: thread t of nt reduces the
+// contiguous slice [n t / nt, n (t + 1) / nt) and the slices' results are
+// combined in thread order, so a run is deterministic for a thread count.
+inline bool par_reduce(idx n) { return g_all && g_threads > 1 && n >= ((idx)1 << 16); }
+
+template <class T, class F> void slices(idx n, std::vector<T>& part, F f) {
+    part.assign(g_threads, T(0));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads)
+    {
+        const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+        part[t] = f(n * t / nt, n * (t + 1) / nt);
+    }
+#else
+    part[0] = f(0, n);
+#endif
+}
+
 // math/linear_view.rs:16-30 (NaN never replaces the running max)
-template <class T> T norm_max(const T* a, idx n) {
+template <class T> T norm_max_range(const T* a, idx lo, idx hi) {
     T m = T(0);
-    for (idx i = 0; i < n; ++i) {
+    for (idx i = lo; i < hi; ++i) {
         const T x = a[i];
         m = x > m ? x : (-x > m ? -x : m);
     }
     return m;
 }
 
+template <class T> T norm_max(const T* a, idx n) {
+    if (!par_reduce(n)) return norm_max_range(a, 0, n);
+    std::vector<T> part;
+    slices(n, part, [&](idx lo, idx hi) { return norm_max_range(a, lo, hi); });
+    T m = T(0);
+    for (T v : part) m = v > m ? v : m;
+    return m;
+}
+
 // math/linear_view.rs:12-14 (ndarray 1-D dot; summation order of ndarray 0.10
-// is not pinned: a serial sum in T is used).
+// is not pinned: a serial sum in T is used, per slice in the all-loops mode).
 template <class T> T dot(const T* a, const T* b, idx n) {
     if (g_dot64) {
+        auto f = [&](idx lo, idx hi) {
+            double s = 0.0;
+            for (idx i = lo; i < hi; ++i) s += (double)a[i] * (double)b[i];
+            return s;
+        };
+        if (!par_reduce(n)) return (T)f(0, n);
+        std::vector<double> part;
+        slices(n, part, f);
         double s = 0.0;
-        for (idx i = 0; i < n; ++i) s += (double)a[i] * (double)b[i];
+        for (double v : part) s += v;
         return (T)s;
     }
+    auto f = [&](idx lo, idx hi) {
+        T s = T(0);
+        for (idx i = lo; i < hi; ++i) s = s + a[i] * b[i];
+        return s;
+    };
+    if (!par_reduce(n)) return f(0, n);
+    std::vector<T> part;
+    slices(n, part, f);
     T s = T(0);
-    for (idx i = 0; i < n; ++i) s = s + a[i] * b[i];
+    for (T v : part) s = s + v;
     return s;
 }
 

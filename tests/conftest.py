@@ -27,7 +27,7 @@ def oracle():
     from oracle import pyoracle
 
     pyoracle.lib()
-    pyoracle.set_threads(min(8, os.cpu_count() or 1), all_loops=True)
+    pyoracle.set_threads(min(16, os.cpu_count() or 1), all_loops=True)
     return pyoracle
 
 

@@ -1,0 +1,93 @@
+"""The benchmarked forms of the step against the FP64 CPU oracle, field by
+field.
+
+The oracle's FP64 step (FP64 fields, Jacobi-PCG to relative 1e-10, every
+loop parallel on the host cores) is the reference result: the restatement
+of examples/dec_fluid.rs:46-141 in double precision, solved far below the
+1e-6 tolerance, so what remains is the error of the GPU form.  Each GPU
+step starts from the same state as the oracle step it is compared with.
+
+Measured on GB300 (the numbers these bounds are set from):
+  * 256^3 headline (filtered-noise velocity, MG-PCG in double-float
+    refinement to 1e-6): velocity 4.5e-6, density 1.9e-6 relative L-inf;
+  * 128^3 sphere + disk plume (MG-PCG in double-float refinement to 1e-6),
+    four steps from rest: see the printed per-step errors.
+The bound for both is 2e-5 relative L-inf: the solve's 1e-6 relative
+residual moves the projected velocity by a few 1e-6 of its maximum, and FP32
+back-trace arithmetic moves the advected density by about 2e-6."""
+
+import numpy as np
+import pytest
+
+from test_gpu_ops import dev, host
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-5  # relative L-inf, velocity and density
+
+
+def rel_linf(a, b):
+    return float(np.abs(a.astype(np.float64) - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def fp64_params(oracle, dt, buoyancy, source_field=None):
+    return oracle.step_params(dt=dt, buoyancy=buoyancy, source_field=source_field, walls_after_advect=True,
+                              zero_solid_after_project=True, precond=1, rel_stop=True, rel_tol=1e-10,
+                              max_iter=1000000)
+
+
+def test_headline_256_cubed_matches_fp64_oracle(pg, oracle):
+    """One step of the 256^3 benchmark configuration (MG-PCG in double-float
+    refinement to relative 1e-6) from its initial state, against the
+    oracle's FP64 step from the same state."""
+    from panopaea_gb300 import workloads as W
+
+    dims = (256, 256, 256)
+    vel, rho = W.initial_state("precision_3d_256", dims)
+    g = pg.Grid3d(dims)
+    gv, gr, gp = pg.Simplex1(g, dev(vel)), pg.Simplex2(g, dev(rho)), g.new_simplex_2()
+    solver = pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4)
+    cfg = pg.StepConfig(dt=1.0, buoyancy=0.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True, solver=solver)
+    st = pg.step(g, cfg, gv, gr, gp)
+    assert st["status"] == 0, st
+    v64, r64, p64 = vel.astype(np.float64), rho.astype(np.float64), np.zeros(dims)
+    so = oracle.step(v64, r64, p64, dims, fp64_params(oracle, 1.0, 0.0))
+    assert so.converged
+    ev, er = rel_linf(host(gv), v64), rel_linf(host(gr), r64)
+    print("256^3: GPU %d iterations, oracle FP64 %d iterations in %.1f s; rel L-inf velocity %.2e density %.2e"
+          % (st["iterations"], so.iterations, so.t_total, ev, er))
+    assert ev <= TOL and er <= TOL, (ev, er)
+
+
+def test_sphere_plume_128_mgpcg_matches_fp64_oracle(pg, oracle):
+    """The large-grid configuration's geometry at 128^3 (solid sphere of
+    radius 16 at the centre, smoke from a bottom disk of radius 8, buoyancy
+    1, dt 0.5, from rest), MG-PCG in double-float refinement to relative
+    1e-6: four steps, each against the oracle's FP64 step from the GPU's
+    state before it."""
+    from panopaea_gb300 import workloads as W
+
+    dims = (128, 128, 128)
+    mask, src = W.sphere_plume(dims)
+    fs = oracle.cell_mask_to_faces(mask)
+    g = pg.Grid3d(dims)
+    g.set_solid_cells(mask)
+    vel, rho = W.initial_state("sphere_3d_512", dims)
+    gv, gr, gp = pg.Simplex1(g, dev(vel)), pg.Simplex2(g, dev(rho)), g.new_simplex_2()
+    gsrc = pg.Simplex2(g, dev(src))
+    solver = pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4)
+    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True, source_field=gsrc, solver=solver)
+    src64 = src.astype(np.float64)
+    prm = fp64_params(oracle, 0.5, 1.0, src64)
+    for i in range(4):
+        v64, r64 = host(gv).astype(np.float64), host(gr).astype(np.float64)
+        p64 = np.zeros(dims)
+        so = oracle.step(v64, r64, p64, dims, prm, fs)
+        st = pg.step(g, cfg, gv, gr, gp)
+        assert st["status"] == 0 and so.converged, (i, st)
+        ev, er = rel_linf(host(gv), v64), rel_linf(host(gr), r64)
+        print("sphere 128^3 step %d: GPU %d iterations, oracle FP64 %d; rel L-inf velocity %.2e density %.2e"
+              % (i, st["iterations"], so.iterations, ev, er))
+        assert ev <= TOL and er <= TOL, (i, ev, er)
