@@ -17,7 +17,7 @@ Two solver forms run on the same workload:
 
 K defaults to 50 (0.24 s of timed work at 256^3, so the clock samples --
 nvidia-smi polled every 50 ms from before the timed region -- fall inside
-it), W to 3; the reference arm defaults to 5 bounded CPU samples.
+it), W to 3.
 
 Multi-GPU (torchrun, one rank per GPU): every rank advances its own replica
 grid (the step has no data-path exchange), `value` = all cells x steps over
@@ -25,7 +25,11 @@ the max time over ranks ("scaling": "weak").
 
 --impl reference times the reference's CPU algorithm (the oracle restatement,
 the reference's threading: derivative_0_dual / derivative_1_primal parallel,
-everything else serial) on the host cores, on a bounded sample per step.
+everything else serial) on the host cores: whole steps, each run to
+convergence and timed, as many as fit in --ref-budget seconds (at least
+one); the same steps with every loop parallel are reported beside them.
+The CPU baseline of the GPU line is one such whole step with every loop
+parallel.
 """
 
 import argparse
@@ -81,7 +85,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-PCG comparison (profiling runs)")
-    ap.add_argument("--cpu-cap", type=int, default=16, help="CG iterations per CPU sample")
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="--impl reference: seconds of timed full CPU steps (at least one step is timed)")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP64 / BF16 precision study")
     ap.add_argument("--pairs", type=int, default=1000, help="learned_3d_128: training pairs (streamed)")
     ap.add_argument("--held", type=int, default=32, help="learned_3d_128: held-out grids")
@@ -328,42 +333,115 @@ def have_mg(pg, grid):
 # ---------------------------------------------------------------------------
 # CPU: the reference algorithm on the host cores (oracle restatement)
 
-def cpu_sample(O, dims, spec, vel0, rho0, cap, n_full=None):
-    """One step of the reference algorithm on the host: advection, RHS and
-    projection in full, the CG truncated at `cap` iterations and its time
-    scaled to the `n_full` iterations the same CG needs to converge (n_full
-    measured untimed with every loop parallel when not given)."""
-    threads = os.cpu_count() or 1
-    dt = spec["dt"]
-    O.set_threads(threads, all_loops=False)  # the reference's threading
+def _threads():
+    return os.cpu_count() or 1
+
+
+def cpu_full_step(O, dims, spec, vel0, rho0, all_loops, src=None, fs=None):
+    """One full step of the reference algorithm on the host, from the given
+    state: inflow, advection, RHS, the reference's CG (identity
+    preconditioner, f32 storage and f32 dot sums, pcg.rs:14-82) run to
+    convergence at the workload's relative tolerance, projection.  Nothing is
+    truncated or extrapolated.  Returns the wall time and the CG's iteration
+    count."""
+    O.set_threads(_threads(), all_loops=all_loops)
     vel = vel0.astype(np.float32).copy()
     rho = rho0.astype(np.float32).copy()
+    p = np.zeros(rho.shape, np.float32)
+    prm = O.step_params(dt=spec["dt"], buoyancy=spec["buoyancy"], source_field=src, walls_after_advect=True,
+                        zero_solid_after_project=True, precond=0, rel_stop=True, rel_tol=spec["rel_tol"],
+                        max_iter=10_000_000)
     t0 = time.perf_counter()
-    rho_n = O.advect(rho, dt, vel, dims)
-    vel_n = O.advect_mac(vel, dt, vel, dims)
-    vel_n = O.walls(vel_n, dims)
-    b = O.divergence_rhs(vel_n, dims)
+    st = O.step(vel, rho, p, dims, prm, fs)
     t1 = time.perf_counter()
-    thr = spec["rel_tol"] * float(np.abs(b).max())
-    tc0 = time.perf_counter()
-    x, _, _, _, it, res, conv = O.pcg(b, dt, dims, cap, thr)
-    tc1 = time.perf_counter()
-    t2 = time.perf_counter()
-    O.project(vel_n, x, dt, dims)
-    t3 = time.perf_counter()
-    t_fixed = (t1 - t0) + (t3 - t2)
-    t_iter = (tc1 - tc0) / max(it, 1)
-    if n_full is None:
-        O.set_threads(threads, all_loops=True)
-        n_full = O.pcg(b, dt, dims, 1000000, thr)[4]
-        O.set_threads(threads, all_loops=False)
-    t_step = t_fixed + n_full * t_iter
+    return {"s": t1 - t0, "iterations": int(st.iterations), "converged": bool(st.converged)}
+
+
+def cpu_timed_steps(O, dims, spec, vel0, rho0, all_loops, max_steps, budget_s):
+    """Full reference steps from the same initial state, timed one by one:
+    at least one, then more while the next (estimated as the last) still
+    fits in budget_s and max_steps is not reached."""
+    runs = []
+    while len(runs) < max(1, max_steps):
+        if runs and sum(r["s"] for r in runs) + runs[-1]["s"] > budget_s:
+            break
+        runs.append(cpu_full_step(O, dims, spec, vel0, rho0, all_loops))
     cells = int(np.prod(dims))
-    return {"value": cells / t_step / 1e6, "t_step_s": t_step, "t_fixed_s": t_fixed, "t_iter_s": t_iter,
-            "n_full": int(n_full), "cap": int(it), "threads": threads, "wall_s": t3 - t0}
+    med = statistics.median(r["s"] for r in runs)
+    return {"value": cells / med / 1e6, "ms_per_step": 1e3 * med, "steps": len(runs),
+            "iterations": [r["iterations"] for r in runs], "converged": all(r["converged"] for r in runs),
+            "seconds": [r["s"] for r in runs]}
+
+
+THREADING = {False: "reference (derivative_0_dual / derivative_1_primal parallel as rayon runs them, the rest "
+                    "serial as written)",
+             True: "every loop parallel, reductions in per-thread slices (a parallelised port, faster than the "
+                   "reference as written)"}
+
+
+def cpu_warmup(O, spec, nd, warmup):
+    """Untimed warm-up of the host path: `warmup` full steps of a 64^3 (64^2)
+    grid, which bring the library and OpenMP's thread pool up."""
+    small = (64,) * nd
+    from panopaea_gb300 import workloads as W
+
+    v, r = W.filtered_noise_velocity(small), (W.filtered_noise_density(small) if nd == 3 else
+                                               W.gaussian_blob_2d(small))
+    for _ in range(warmup):
+        cpu_full_step(O, small, spec, v, r, False)
+
+
+def oracle_fp64_step(O, dims, spec, vel0, rho0):
+    """The all-FP64 oracle step (FP64 fields, Jacobi-PCG to relative 1e-10,
+    every loop parallel) from the initial state: the reference result of the
+    precision study."""
+    O.set_threads(_threads(), all_loops=True)
+    v = vel0.astype(np.float64)
+    r = rho0.astype(np.float64)
+    p = np.zeros(r.shape)
+    prm = O.step_params(dt=spec["dt"], buoyancy=spec["buoyancy"], walls_after_advect=True,
+                        zero_solid_after_project=True, precond=1, rel_stop=True, rel_tol=1e-10, max_iter=10_000_000)
+    t0 = time.perf_counter()
+    st = O.step(v, r, p, dims, prm)
+    return v, r, {"form": "CPU oracle: FP64 fields, FP64 Jacobi-PCG to relative 1e-10, every loop parallel",
+                  "s": time.perf_counter() - t0, "iterations": int(st.iterations), "threads": _threads()}
+
+
+def cpu_leg(O, dims, spec, vel0, rho0, prec_fields):
+    """Rank 0, N = 1: the CPU baseline -- one full step of the reference
+    algorithm with every loop parallel on the host cores, measured (a
+    bounded sample of the workload: one step) -- and, for the precision
+    study, the oracle's all-FP64 step from the same initial state, against
+    which the GPU forms' fields are compared."""
+    cpu_warmup(O, spec, len(dims), 1)
+    b = cpu_timed_steps(O, dims, spec, vel0, rho0, True, 1, 0.0)
+    cpu = {"value": b["value"], "unit": UNIT, "cores": _threads(), "kind": "port",
+           "sample": "one full %s step from the initial state (inflow, advection, RHS, the reference's "
+                     "unpreconditioned CG in f32 to relative %g: %d iterations, projection), measured, nothing "
+                     "extrapolated; threading: %s" % ("x".join(map(str, dims)), spec["rel_tol"],
+                                                       b["iterations"][0], THREADING[True]),
+           "ms_per_step": b["ms_per_step"], "iterations": b["iterations"][0], "extrapolated": False}
+    oracle64 = None
+    if prec_fields is not None:
+        v64, r64, info = oracle_fp64_step(O, dims, spec, vel0, rho0)
+
+        def rel(a, b_):
+            a, b_ = a.ravel(), b_.ravel()
+            return float(np.abs(a - b_).max() / max(np.abs(b_).max(), 1e-300))
+
+        oracle64 = dict(info)
+        for k, (gv, gr) in prec_fields.items():
+            oracle64[k] = {"velocity_rel_linf": rel(gv, v64), "density_rel_linf": rel(gr, r64)}
+    return cpu, oracle64
 
 
 def reference_arm(args, spec, dims):
+    """The reference's CPU algorithm (the oracle restatement) on the host
+    cores, full steps measured one by one from the workload's initial state.
+    `value` uses the reference's own threading; the same steps with every
+    loop parallel are reported beside it.  Warm-up: `--warmup` untimed full
+    steps of a 64^3 grid; the timed steps run until --ref-budget seconds
+    would be exceeded (at least one)."""
     ws, rank, local = dist_setup()
     if rank != 0:
         return
@@ -371,24 +449,27 @@ def reference_arm(args, spec, dims):
     from panopaea_gb300 import workloads as W
 
     vel0, rho0 = W.initial_state(args.workload, dims)
-    n_full = None
-    vals = []
-    for i in range(args.warmup + args.steps):
-        s = cpu_sample(O, dims, spec, vel0, rho0, args.cpu_cap, n_full)
-        n_full = s["n_full"]
-        if i >= args.warmup:
-            vals.append(s)
-    value = statistics.median(v["value"] for v in vals)
-    sample = ("one %s step per bench step: advection, RHS, projection in full, CG truncated at %d iterations, "
-              "time scaled to the %d iterations the reference CG needs (measured untimed)" %
-              ("x".join(map(str, dims)), vals[0]["cap"], n_full))
+    cpu_warmup(O, spec, len(dims), args.warmup)
+    ref = cpu_timed_steps(O, dims, spec, vel0, rho0, False, args.steps, args.ref_budget)
+    par = cpu_timed_steps(O, dims, spec, vel0, rho0, True, args.steps, args.ref_budget / 2)
+    value = ref["value"]
+    sample = ("%d full %s step(s) from the initial state, each timed whole: inflow, advection, RHS, the "
+              "reference's unpreconditioned CG in f32 (f32 dot sums) to relative %g (%s iterations), "
+              "projection; nothing extrapolated; warm-up %d untimed 64^3 steps" %
+              (ref["steps"], "x".join(map(str, dims)), spec["rel_tol"], ref["iterations"], args.warmup))
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(v["t_step_s"] for v in vals),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "steps": ref["steps"], "requested_steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ref["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "dims": list(dims), "form": "reference CG (identity preconditioner)",
-                   "threading": "reference (rayon loops parallel, rest serial)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": vals[0]["threads"], "kind": "port", "sample": sample},
+                   "threading": THREADING[False]},
+        "iterations_per_step": ref["iterations"], "seconds_per_step": ref["seconds"],
+        "all_loops_parallel": {"value": par["value"], "unit": UNIT, "ms_per_step": par["ms_per_step"],
+                               "steps": par["steps"], "iterations_per_step": par["iterations"],
+                               "threading": THREADING[True]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": _threads(), "kind": "port", "sample": sample,
+                         "extrapolated": False},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -425,16 +506,20 @@ def precision_study(torch, pg, grid, spec, vel0, rho0, chosen, src):
     s64 = pg.SolverConfig(precond=1, rel_stop=True, rel_tol=1e-10, max_iter=200000)
     cfg64 = step_cfg(pg, spec, s64, None)
     v64, r64, st64, t64 = one(torch.from_numpy(vel0).double().cuda(), torch.from_numpy(rho0).reshape(grid.dim()).double().cuda(), cfg64)
-    return {
+    study = {
         "step": "one step from the initial state",
-        "fp64_reference": {"form": "FP64 fields, FP64 Jacobi-PCG to relative 1e-10", "ms": t64,
-                           "iterations": st64["iterations"]},
-        "fp32_refined": {"velocity_rel_linf_vs_fp64": rel(v32, v64), "density_rel_linf_vs_fp64": rel(r32, r64),
+        "fp64_gpu": {"form": "this library's FP64 entry points: FP64 fields, FP64 Jacobi-PCG to relative 1e-10",
+                     "ms": t64, "iterations": st64["iterations"]},
+        "fp32_refined": {"velocity_rel_linf_vs_fp64_gpu": rel(v32, v64), "density_rel_linf_vs_fp64_gpu": rel(r32, r64),
                          "ms": t32, "iterations": s32["iterations"],
                          "true_residual_rel": s32["true_residual_max"] / s32["b_max"] if s32["b_max"] else 0.0},
-        "bf16_density": {"velocity_rel_linf_vs_fp64": rel(vb, v64), "density_rel_linf_vs_fp64": rel(rb, r64),
+        "bf16_density": {"velocity_rel_linf_vs_fp64_gpu": rel(vb, v64), "density_rel_linf_vs_fp64_gpu": rel(rb, r64),
                          "density_rel_linf_vs_fp32": rel(rb, r32), "ms": tb, "iterations": sb["iterations"]},
     }
+    # host copies for the comparison with the CPU oracle's FP64 step
+    fields = {k: (v.cpu().numpy(), r.cpu().numpy().ravel()) for k, (v, r) in
+              {"fp32_refined": (v32, r32), "bf16_density": (vb, rb), "fp64_gpu": (v64, r64)}.items()}
+    return study, fields
 
 
 def timed_steps(torch, pg, dist, grid, cfg, gv, gr, gp, k):
@@ -518,19 +603,22 @@ def ours(args, spec, dims):
     plain_out = None
     if not args.no_plain:
         gv2, gr2, gp2 = fresh()
-        pg.step(grid, cfg_p, gv2, gr2, gp2)  # warm-up
+        st_first = pg.step(grid, cfg_p, gv2, gr2, gp2)  # warm-up, from the initial state
         kp = args.plain_steps or max(1, min(args.steps, 3))
         ms_p, st_p = timed_steps(torch, pg, dist, grid, cfg_p, gv2, gr2, gp2, kp)
         ms_p = dist.max(ms_p)
         value_plain = ws * cells * kp / (ms_p / 1e3) / 1e6
         plain_out = {"value": value_plain, "unit": UNIT, "ms_per_step": ms_p / kp,
-                     "iterations_per_step": [s["iterations"] for s in st_p], "speedup_of_chosen": value / value_plain}
+                     "iterations_per_step": [s["iterations"] for s in st_p], "speedup_of_chosen": value / value_plain,
+                     "iterations_first_step": st_first["iterations"],
+                     "sums": "FP64-class dot products (the CPU reference sums in f32 and needs more iterations "
+                             "from the same state: see cpu_baseline.iterations)"}
         del gv2, gr2, gp2
     # --- precision study (256^3): FP32 storage + refinement and BF16-stored
     # density against an all-FP64 step on the same initial state -----------
-    precision = None
+    precision, prec_fields = None, None
     if not args.no_precision and spec.get("cpu") and len(dims) == 3:
-        precision = precision_study(torch, pg, grid, spec, vel0, rho0, chosen, src)
+        precision, prec_fields = precision_study(torch, pg, grid, spec, vel0, rho0, chosen, src)
     # --- e2e through the public API with host buffers ---------------------
     e2e = None
     if not args.no_e2e:
@@ -558,12 +646,10 @@ def ours(args, spec, dims):
     if rank == 0 and ws == 1 and not args.no_cpu and spec.get("cpu"):
         from oracle import pyoracle as O
 
-        s = cpu_sample(O, dims, spec, vel0, rho0, args.cpu_cap)
-        cpu = {"value": s["value"], "unit": UNIT, "cores": s["threads"], "kind": "port",
-               "sample": "one %s step: advection, RHS, projection in full (reference threading), CG truncated at %d "
-                         "iterations and scaled to the %d the reference CG needs (counted untimed, all loops "
-                         "parallel); %.1f s of CPU wall time" % ("x".join(map(str, dims)), s["cap"], s["n_full"],
-                                                                 s["wall_s"])}
+        cpu, oracle64 = cpu_leg(O, dims, spec, vel0, rho0, prec_fields)
+        if precision is not None and oracle64 is not None:
+            precision["fp64_oracle"] = oracle64
+    del prec_fields
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

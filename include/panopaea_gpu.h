@@ -258,11 +258,15 @@ int pg_pcg_f64(const pg_grid* grid, int precond, double* x, const double* b, int
  * process exits), so grids are limited to 1,048,576 cells; larger grids
  * are rejected with PG_BAD_ARG.  The first call on each device looks the
  * array's device address up (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Every call
- * shares the array and overwrites what the previous call left there (the
- * state is cleared at the start of each call), so calls that overlap on the
- * GPU -- on different streams, or from different threads -- race.  It
- * calls no cudaMalloc, cudaFree or allocating library routine. */
+ * current and keeps it for the life of the process; make that first call
+ * before any stream capture.  A cudaDeviceReset ends the context that
+ * address belongs to: after one, make no further call of this entry point
+ * on that device.  Every call shares the array and overwrites what the
+ * previous call left there (the state is cleared at the start of each
+ * call), so calls that overlap on the GPU -- on different streams, or from
+ * different threads -- race.  The call reads the solver state back to the
+ * host while it iterates and synchronises cuda_stream before it returns.
+ * It calls no cudaMalloc, cudaFree or allocating library routine. */
 int pg_pcg_noalloc_f32(int32_t nd, int64_t d, int64_t h, int64_t w, const uint8_t* cell_flags, int precond,
                        float* x, const float* b, int64_t max_iterations, double threshold, float* residual,
                        float* auxiliary, float* search, double dt, void* cuda_stream, pg_pcg_stats* stats);
@@ -459,6 +463,16 @@ int pg_profile_read(int kind, double* total_ms, int64_t* launches);
  * microseconds): those of at least the smaller of a quarter of the kind's
  * longest launch and the geometric mean of its shortest and longest. */
 int pg_profile_read_active(int kind, double* total_ms, int64_t* launches);
+
+/* Test hook (no reference counterpart): the poll budget of the TMA
+ * pipeline-stage waits of the z-marching kernels.  0 makes every stage wait
+ * give up at once, so the give-up path runs without any fault: the block
+ * waits (bounded) for its copies in flight, sets PG_TIMEOUT and stops the
+ * solve.  A solve that returns PG_TIMEOUT has untrustworthy results; the
+ * next solve starts from a fresh state.  Synchronous; restore the budget
+ * with pg_debug_stage_wait_polls_default(). */
+int pg_debug_set_stage_wait_polls(uint32_t polls);
+uint32_t pg_debug_stage_wait_polls_default(void);
 
 #ifdef __cplusplus
 }

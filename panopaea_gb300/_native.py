@@ -100,6 +100,8 @@ _I = C.c_int
 # name -> (restype, argtypes)
 _SIGS = {
     "pg_status_string": (C.c_char_p, [_I]),
+    "pg_debug_set_stage_wait_polls": (_I, [C.c_uint32]),
+    "pg_debug_stage_wait_polls_default": (C.c_uint32, []),
     "pg_last_error": (C.c_char_p, []),
     "pg_version": (_I, []),
     "pg_grid_create_2d": (_I, [_I64, _I64, C.POINTER(_P)]),

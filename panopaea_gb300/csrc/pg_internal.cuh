@@ -154,7 +154,7 @@ struct CgState {
 
 // Host view of the workspace owned by a grid.
 struct Workspace {
-    double* partials = nullptr;  // per-block reduction partials (2 x kMaxBlocks)
+    double* partials = nullptr;  // per-block reduction partials (4 x kMaxBlocks: two reductions of two kernels)
     CgState* state = nullptr;    // device
     CgState* state_host = nullptr;  // pinned mirror
     void* vec = nullptr;         // extra CG vectors (lazily sized)

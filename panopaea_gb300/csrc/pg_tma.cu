@@ -42,3 +42,11 @@ bool encode_map_3d(CUtensorMap* map, const void* base, int elem, i64 w, i64 h, i
 }
 
 }  // namespace pg
+
+extern "C" int pg_debug_set_stage_wait_polls(uint32_t polls) {
+    int rc = pg::set_stage_wait_polls_spmv(polls);
+    if (rc == PG_OK) rc = pg::set_stage_wait_polls_mg(polls);
+    return rc;
+}
+
+extern "C" uint32_t pg_debug_stage_wait_polls_default(void) { return pg::kMbarSpinLimit; }

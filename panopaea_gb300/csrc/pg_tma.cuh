@@ -59,18 +59,31 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-// Wait for the phase with the given parity to complete; false once
-// kMbarSpinLimit polls or kMbarWaitNs nanoseconds have passed.
+// Poll budget of the pipeline-stage waits below: kMbarSpinLimit, or 0 set
+// through pg_debug_set_stage_wait_polls, with which every stage wait gives
+// up at once -- the way a test drives the give-up path (drain the copies in
+// flight, report PG_TIMEOUT) without any fault.  Each translation unit that
+// waits keeps its own copy (set_stage_wait_polls_* below).
+static __constant__ unsigned c_stage_wait_polls = kMbarSpinLimit;
+
+// Wait for the phase with the given parity to complete; false once the poll
+// budget or kMbarWaitNs nanoseconds have passed.
 constexpr uint64_t kMbarWaitNs = 500000000ull;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    const unsigned limit = c_stage_wait_polls;
+    if (limit == 0) return false;
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
-    for (unsigned k = 0; k < kMbarSpinLimit; ++k) {
+    for (unsigned k = 0; k < limit; ++k) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((k & 255) == 255 && global_ns() - t0 > kMbarWaitNs) return false;
     }
     return false;
 }
+
+// Host: the stage-wait poll budget of pg_spmv.cu's and pg_mg.cu's kernels.
+int set_stage_wait_polls_spmv(unsigned polls);
+int set_stage_wait_polls_mg(unsigned polls);
 
 // 3D tiled load of the box at (x, y, z) into shared memory, completing on bar.
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
@@ -83,6 +96,39 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 
 __device__ __forceinline__ void tma_prefetch_map(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
+}
+
+// Work split of the z-marching kernels: the ntiles * d plane-tiles of a
+// grid, ordered tile by tile (each tile's column of planes in z order), are
+// cut into gridDim.x equal contiguous ranges, so every block of a launch
+// sized to the resident blocks has the same number of planes to compute.  A
+// block walks its range as one item per tile column it touches: planes
+// [z0, z1) of tile `tile`.
+struct ZWalk {
+    int pos, hi, d;
+    __device__ __forceinline__ ZWalk(int ntiles, int d_) : d(d_) {
+        const i64 total = (i64)ntiles * d_;
+        pos = (int)(total * blockIdx.x / gridDim.x);
+        hi = (int)(total * (blockIdx.x + 1) / gridDim.x);
+    }
+    __device__ __forceinline__ bool next(int& tile, int& z0, int& z1) {
+        if (pos >= hi) return false;
+        tile = pos / d;
+        z0 = pos - tile * d;
+        z1 = min(d, z0 + (hi - pos));
+        pos += z1 - z0;
+        return true;
+    }
+};
+
+// Blocks of a z-marching launch: every resident block (cap), but no fewer
+// than kZMinPlanes planes per block.
+constexpr int kZMinPlanes = 8;
+inline int zwalk_blocks(int ntiles, i64 d, int cap) {
+    const i64 total = (i64)ntiles * d;
+    i64 nb = total / kZMinPlanes;
+    if (nb > cap) nb = cap;
+    return nb < 1 ? 1 : (int)nb;
 }
 
 // Host: encode a 3D tiled map over a dense (d, h, w) array of elem-byte

@@ -110,5 +110,7 @@ def main(ref_root):
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--header":
         write_header()
+    elif len(sys.argv) == 2:
+        main(sys.argv[1])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+        sys.exit("usage: python tests/golden/make_golden.py <reference-root> | --header")

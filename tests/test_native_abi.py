@@ -104,6 +104,22 @@ def test_status_strings(lib):
     assert L.pg_version() >= 1
 
 
+def test_timeout_status_is_distinct(lib):
+    """PG_TIMEOUT (a bounded device wait gave up; the solve's results are
+    not to be trusted) has its own code, string and Python error, distinct
+    from non-convergence, NaN and breakdown -- checked on the host, no GPU."""
+    L = lib.load()
+    codes = [lib.PG_OK, lib.PG_NOT_CONVERGED, lib.PG_NAN_DETECTED, lib.PG_TIMEOUT, lib.PG_BAD_ARG,
+             lib.PG_CUDA_ERROR, lib.PG_NO_DEVICE, lib.PG_OUT_OF_MEMORY, lib.PG_BREAKDOWN]
+    assert len(set(codes)) == len(codes)
+    strings = [L.pg_status_string(c) for c in codes]
+    assert len(set(strings)) == len(strings) and L.pg_status_string(lib.PG_TIMEOUT) == b"PG_TIMEOUT"
+    with pytest.raises(lib.PgError) as ei:
+        lib.check(lib.PG_TIMEOUT, allow=(lib.PG_OK, lib.PG_NOT_CONVERGED))
+    assert ei.value.status == lib.PG_TIMEOUT and str(ei.value).startswith("PG_TIMEOUT")
+    assert L.pg_debug_stage_wait_polls_default() > 0
+
+
 def test_no_device_fails_loudly(lib):
     """Without a GPU the library refuses to run rather than computing on the host."""
     import torch
