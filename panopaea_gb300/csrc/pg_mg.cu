@@ -66,7 +66,8 @@ struct MgHierarchy {
     float* e0b = nullptr;
     CUtensorMap gmap;  // level-0 flags
     CUtensorMap cmap;  // level-1 correction (prolongation)
-    int pair_cap = 0;  // resident k_mg_pair blocks on the device
+    int pair_cap = 0;          // resident k_mg_pair blocks on the device (every mode)
+    int pair_cap_plain = 0;    // the same for the modes without the coarse correction
     struct MapEnt {
         const void* p = nullptr;
         int by = 0;
@@ -272,7 +273,7 @@ struct PairArgs {
     float dt;
     float* eout;
     int c1;  // colour of the first half-sweep
-    int tiles_x, tiles_y, zc, nwork;
+    int tiles_x, tiles_y;
 };
 
 template <int M1, bool RZ>
@@ -348,10 +349,10 @@ __global__ void __launch_bounds__(kPThreads, kPMinBlocks)
     unsigned seq = 0;     // planes this block has consumed: ring slot and phase parity
     bool failed = false;  // block-uniform: a wait gave up
     Acc<float> acc, zs;   // z.r and sum(z) (RZ)
-    for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
-        const int tz = item / per_plane, t2 = item - tz * per_plane;
+    ZWalk walk(per_plane, d);
+    int t2, z0, z1;
+    while (!failed && walk.next(t2, z0, z1)) {
         const int x0 = (t2 % a.tiles_x) * kPX, y0 = (t2 / a.tiles_x) * kPY;
-        const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
         const int n = z1 - z0 + 4;  // planes z0 - 2 .. z1 + 1 (ring index j = plane - z0 + 2)
         if (tid == 0)
             for (int j = 0; j < min(n, kStages); ++j) issue(seq + j, z0 - 2 + j, x0, y0);
@@ -903,6 +904,11 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
     return PG_OK;
 }
 
+int set_stage_wait_polls_mg(unsigned polls) {
+    PG_CUDA(cudaMemcpyToSymbol(c_stage_wait_polls, &polls, sizeof(polls)));
+    return PG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Fused fine-level pairs: launch setup.
 
@@ -918,12 +924,20 @@ static int pair_setup(pg_grid* g, MgHierarchy* H) {
     int e = pair_attr<PR_SELF, false>() | pair_attr<PR_PLAIN, false>() | pair_attr<PR_PROLONG, false>() |
             pair_attr<PR_PLAIN, true>() | pair_attr<PR_PROLONG, true>();
     if (e) return cuda_fail((cudaError_t)e, "cudaFuncSetAttribute(k_mg_pair)");
-    int bps = 0, bps2 = 0;
-    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_mg_pair<PR_PLAIN, false>, kPThreads,
+    int bps[5] = {};
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[0], k_mg_pair<PR_PLAIN, false>, kPThreads,
                                                           PairCfg<PR_PLAIN>::kSmem));
-    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps2, k_mg_pair<PR_PROLONG, false>, kPThreads,
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[1], k_mg_pair<PR_PLAIN, true>, kPThreads,
+                                                          PairCfg<PR_PLAIN>::kSmem));
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[2], k_mg_pair<PR_SELF, false>, kPThreads,
+                                                          PairCfg<PR_SELF>::kSmem));
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[3], k_mg_pair<PR_PROLONG, false>, kPThreads,
                                                           PairCfg<PR_PROLONG>::kSmem));
-    H->pair_cap = std::min(std::min(bps, bps2) * g->num_sms, kMaxBlocks);
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[4], k_mg_pair<PR_PROLONG, true>, kPThreads,
+                                                          PairCfg<PR_PROLONG>::kSmem));
+    const int plain = std::min(bps[0], std::min(bps[1], bps[2]));
+    H->pair_cap_plain = std::min(plain * g->num_sms, kMaxBlocks);
+    H->pair_cap = std::min(std::min(plain, std::min(bps[3], bps[4])) * g->num_sms, kMaxBlocks);
     const MgLevel& C = H->lv[1];
     if (!encode_map_3d(&H->cmap, C.e, 4, C.D.w, C.D.h, C.D.d, kPCw, kPCh)) H->pair_cap = 0;
     return PG_OK;
@@ -946,7 +960,7 @@ static const CUtensorMap* vec_map(const MgHierarchy& H, const float* p, int by) 
 struct PairLaunch {
     const CUtensorMap* fm;  // f (the residual r)
     PairArgs a;
-    int nb;
+    int nb_plain, nb_prolong;  // blocks of the launches without / with the coarse correction
 };
 
 // Geometry of the pair launches of one V-cycle; false when a vector cannot
@@ -962,21 +976,19 @@ static bool pair_plan(const MgHierarchy& H, const float* r, const float* z, Pair
     a.dt = (float)H.dt;
     a.tiles_x = (a.w + kPX - 1) / kPX;
     a.tiles_y = (a.h + kPY - 1) / kPY;
-    const int tiles = a.tiles_x * a.tiles_y;
-    // one work item per resident block, chunks of at least 8 planes
-    const int nch = std::max(1, std::min(H.pair_cap / tiles, (a.d + 7) / 8));
-    a.zc = (a.d + nch - 1) / nch;
-    a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
-    P->nb = std::max(1, std::min(a.nwork, H.pair_cap));
+    // every resident block, each with an equal share of the plane-tiles
+    P->nb_plain = zwalk_blocks(a.tiles_x * a.tiles_y, a.d, H.pair_cap_plain);
+    P->nb_prolong = zwalk_blocks(a.tiles_x * a.tiles_y, a.d, H.pair_cap);
     return true;
 }
 
 template <int M1, bool RZ>
 static void pair_t(pg_grid* g, const MgHierarchy& H, const CUtensorMap* em, const PairLaunch& P, const PairArgs& a) {
     cudaStream_t s = g->stream;
+    const int nb = M1 == PR_PROLONG ? P.nb_prolong : P.nb_plain;
     PG_LAUNCH(KK_MG_PAIR, s,
-              k_mg_pair<M1, RZ><<<P.nb, kPThreads, PairCfg<M1>::kSmem, s>>>(*em, *P.fm, H.gmap, H.cmap, a,
-                                                                            g->ws.state, g->ws.partials));
+              k_mg_pair<M1, RZ><<<nb, kPThreads, PairCfg<M1>::kSmem, s>>>(*em, *P.fm, H.gmap, H.cmap, a,
+                                                                          g->ws.state, g->ws.partials));
 }
 
 // One fused pair: first half-sweep over colour c1 in `mode` from ein

@@ -48,7 +48,7 @@ struct SpmvArgs {
     float* p0;
     float* p1;
     float* ap;
-    int tiles_x, tiles_y, zc, nwork;
+    int tiles_x, tiles_y;
 };
 
 template <int PM>
@@ -119,10 +119,10 @@ __global__ void __launch_bounds__(kSThreads, 2)
     unsigned seq = 0;
     bool failed = false;
     Acc<float> acc;
-    for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
-        const int tz = item / per_plane, t2 = item - tz * per_plane;
+    ZWalk walk(per_plane, d);
+    int t2, z0, z1;
+    while (!failed && walk.next(t2, z0, z1)) {
         const int x0 = (t2 % a.tiles_x) * kSX, y0 = (t2 / a.tiles_x) * kSY;
-        const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
         const int n = z1 - z0 + 2;  // planes z0 - 1 .. z1 (ring index j = plane - z0 + 1)
         if (tid == 0)
             for (int j = 0; j < min(n, kSStages); ++j) issue(seq + j, z0 - 1 + j, x0, y0);
@@ -262,7 +262,7 @@ struct ResArgs {
     int d, h, w;
     float dt;
     float* r;
-    int tiles_x, tiles_y, zc, nwork;
+    int tiles_x, tiles_y;
 };
 
 __global__ void __launch_bounds__(kRThreads, 2)
@@ -309,10 +309,10 @@ __global__ void __launch_bounds__(kRThreads, 2)
     unsigned seq = 0;
     bool failed = false;
     float m = 0.f;
-    for (int item = blockIdx.x; item < a.nwork && !failed; item += gridDim.x) {
-        const int tz = item / per_plane, t2 = item - tz * per_plane;
+    ZWalk walk(per_plane, d);
+    int t2, z0, z1;
+    while (!failed && walk.next(t2, z0, z1)) {
         const int x0 = (t2 % a.tiles_x) * kRX, y0 = (t2 / a.tiles_x) * kRY;
-        const int z0 = tz * a.zc, z1 = min(z0 + a.zc, d);
         const int n = z1 - z0 + 2;  // planes z0 - 1 .. z1 (ring index j = plane - z0 + 1)
         if (tid == 0)
             for (int j = 0; j < min(n, kRStages); ++j) issue(seq + j, z0 - 1 + j, x0, y0);
@@ -460,6 +460,11 @@ template <int PM> static int spmv_cap(int num_sms) {
 
 }  // namespace
 
+int set_stage_wait_polls_spmv(unsigned polls) {
+    PG_CUDA(cudaMemcpyToSymbol(c_stage_wait_polls, &polls, sizeof(polls)));
+    return PG_OK;
+}
+
 bool spmv_tma_launch(cudaStream_t s, int num_sms, int pm, const float* zb, float* p0, float* p1, float* ap,
                      const uint8_t* flags, const Dims& D, float dt, CgState* st, double* partials) {
     if (pm != PM_NONE && pm != PM_JACOBI && pm != PM_ZBUF) return false;
@@ -481,11 +486,7 @@ bool spmv_tma_launch(cudaStream_t s, int num_sms, int pm, const float* zb, float
     a.ap = ap;
     a.tiles_x = (a.w + kSX - 1) / kSX;
     a.tiles_y = (a.h + kSY - 1) / kSY;
-    const int tiles = a.tiles_x * a.tiles_y;
-    const int nch = std::max(1, std::min(cap / tiles, (a.d + 7) / 8));
-    a.zc = (a.d + nch - 1) / nch;
-    a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
-    const int nb = std::max(1, std::min(a.nwork, cap));
+    const int nb = zwalk_blocks(a.tiles_x * a.tiles_y, a.d, cap);
     if (pm == PM_ZBUF)
         k_cg_spmv3p<PM_ZBUF><<<nb, kSThreads, kSSmem, s>>>(zm, pm0, pm1, gm, a, st, partials);
     else if (pm == PM_JACOBI)
@@ -522,11 +523,7 @@ bool residual_df_tma_launch(cudaStream_t s, int num_sms, const float* b, const f
     a.r = r;
     a.tiles_x = (a.w + kRX - 1) / kRX;
     a.tiles_y = (a.h + kRY - 1) / kRY;
-    const int tiles = a.tiles_x * a.tiles_y;
-    const int nch = std::max(1, std::min(cap / tiles, (a.d + 7) / 8));
-    a.zc = (a.d + nch - 1) / nch;
-    a.nwork = tiles * ((a.d + a.zc - 1) / a.zc);
-    const int nb = std::max(1, std::min(a.nwork, cap));
+    const int nb = zwalk_blocks(a.tiles_x * a.tiles_y, a.d, cap);
     k_residual_df3p<<<nb, kRThreads, kRSmem, s>>>(hm, lm, bm, gm, a, partials, counter, out, st);
     return true;
 }
