@@ -88,8 +88,8 @@ def parse_args():
     ap.add_argument("--ref-budget", type=float, default=150.0,
                     help="--impl reference: seconds of timed full CPU steps (at least one step is timed)")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP64 / BF16 precision study")
-    ap.add_argument("--pairs", type=int, default=1000, help="learned_3d_128: training pairs (streamed)")
-    ap.add_argument("--held", type=int, default=32, help="learned_3d_128: held-out grids")
+    ap.add_argument("--pairs", type=int, default=10000, help="learned_3d_128: training pairs (streamed)")
+    ap.add_argument("--held", type=int, default=256, help="learned_3d_128: held-out grids")
     ap.add_argument("--gen", default="mg", choices=["mg", "plain"], help="learned_3d_128: solver of the pairs")
     ap.add_argument("--batch-count", type=int, default=512, help="batch_512: number of grids")
     args = ap.parse_args()
@@ -701,10 +701,11 @@ def bf16_peak():
 def bench_learned(args):
     """128^3 grids, 1-6 solid boxes, filtered-noise divergence.  The network
     is trained on --pairs freshly generated (b, p) pairs (streamed), then
-    --held held-out grids are solved to relative 1e-6 by plain CG and by
-    MG-PCG (both in FP64 refinement), each from x = 0 and from the learned
-    guess.  A step = one pressure solve; value = the learned-guess + plain
-    CG form; every form is reported."""
+    --held held-out grids are solved to relative 1e-6 (FP64-class
+    refinement) by plain CG and by MG-PCG, each from x = 0 and from the
+    learned guess, by Jacobi-PCG, and by the flexible CG with the network
+    inside as a preconditioner correction.  A step = one pressure solve;
+    value = the learned-guess + plain CG form; every form is reported."""
     import ctypes as C
 
     import torch
@@ -736,7 +737,17 @@ def bench_learned(args):
         "mg_pcg": (pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=4), None),
         "learned_guess_mg_pcg": (pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=20000,
                                                  refine=4), 0),
+        # the network inside the CG: flexible CG with z = a net(r) + D^-1 (r - a A net(r))
+        "learned_precond_fcg": (pg.SolverConfig(rel_stop=True, rel_tol=1e-6, max_iter=100000, refine=8), "pc"),
+        "jacobi_pcg": (pg.SolverConfig(precond=1, rel_stop=True, rel_tol=1e-6, max_iter=100000, refine=8), None),
     }
+
+    def run_form(solver, corr, b):
+        if corr is None:
+            return pg.solve_pressure(g, x, b, dt, solver)
+        if corr == "pc":
+            return learned.solve_learned_pcg(net, g, x, b, dt, solver)
+        return learned.solve_with_guess(net, g, x, b, dt, solver, corr)
     res = {k: {"ms": [], "iterations": [], "true_residual_rel": []} for k in forms}
     held = [learned.training_pair(g, 9_000_000 + i, dt, solve=False)[::2] for i in range(args.held)]
     stream = torch.cuda.current_stream()
@@ -745,20 +756,27 @@ def bench_learned(args):
     g.set_solid_cells(held[0][1])
     for name, (solver, corr) in forms.items():
         for _ in range(2):
-            (pg.solve_pressure(g, x, held[0][0], dt, solver) if corr is None
-             else learned.solve_with_guess(net, g, x, held[0][0], dt, solver, corr))
+            run_form(solver, corr, held[0][0])
     clocks = Clocks(local)
     clocks.start()
     launches0 = lib.pg_kernel_launches()
     dist.barrier()
+    setup_ms = []
     for b, mask in held:
         g.set_solid_cells(mask)
+        # untimed: the multigrid hierarchy of the new mask (its build is reported as setup_ms)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        pg.solve_pressure(g, x, b, dt, forms["mg_pcg"][0])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        setup_ms.append(e0.elapsed_time(e1))
         for name, (solver, corr) in forms.items():
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record(stream)
-            st = (pg.solve_pressure(g, x, b, dt, solver) if corr is None
-                  else learned.solve_with_guess(net, g, x, b, dt, solver, corr))
+            st = run_form(solver, corr, b)
             e1.record(stream)
             torch.cuda.synchronize()
             res[name]["ms"].append(e0.elapsed_time(e1))
@@ -820,6 +838,7 @@ def bench_learned(args):
                        "form": "learned guess + 1 learned correction, then plain CG in FP64 refinement",
                        "parallelism": "replicas x%d" % ws, "l2": "fields of 8 MB per grid: L2-resident"},
             "forms": out_forms,
+            "mg_setup_and_first_solve_ms": float(np.mean(setup_ms)),
             "speedup_vs_plain_cg": out_forms["plain_cg"]["ms_per_solve"] / out_forms["learned_guess_plain_cg"]["ms_per_solve"],
             "iterations_saved_vs_plain_cg": 1.0 - out_forms["learned_guess_plain_cg"]["mean_iterations"] /
             out_forms["plain_cg"]["mean_iterations"],

@@ -443,6 +443,16 @@ int pg_unet_forward_f32(pg_unet* net, const pg_grid* grid, const float* b, doubl
  * corrections > 0 repeats it on the residual (x += alpha d, d = net(b - Ax)).
  * Asynchronous. */
 int pg_unet_guess_f32(pg_unet* net, const pg_grid* grid, const float* b, double dt, int corrections, float* x);
+/* Pressure solve A x = b whose preconditioner is the network plus a Jacobi
+ * step (no reference counterpart; it takes the place of the `Preconditioner`
+ * of pcg.rs:4-6): for a residual r, q = net(r), a = (q.r) / (q.Aq) and
+ * z = a q + D^-1 (r - a A q).  z depends on r non-linearly, so the CG is
+ * the flexible one (Polak-Ribiere beta); it runs to params' tolerance,
+ * inside FP64-class refinement when params->refine > 0, so the result's
+ * accuracy does not depend on the network.  params->precond is not used.
+ * Synchronous; returns the solve's status. */
+int pg_solve_pressure_learned_f32(const pg_grid* grid, const pg_solver_params* params, pg_unet* net, float* x,
+                                  const float* b, double dt, pg_pcg_stats* stats);
 
 /* ----------------------------------------------------------------------- */
 /* Instrumentation (no reference counterpart; the reference only prints

@@ -703,6 +703,7 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
                                                          cfg.rel_tol, cfg.max_iter, cfg.zero_x, ws.state,
                                                          ws.partials, cfg.nfluid));
     PG_CHECK_LAUNCH();
+    if (PM == PM_ZBUF) hook->bind(buf.ap);
     if (PM == PM_ZBUF && (rc = hook->apply(g, buf.r, buf.z))) return rc;
     // Device-side loop: one graph launch runs every iteration.
     CgGraph* G = nullptr;

@@ -72,6 +72,9 @@ struct ZHook {
     virtual int apply(pg_grid* g, const void* r, void* z) = 0;
     // Identity of the kernel sequence apply() enqueues (graph cache key).
     virtual uintptr_t key() const = 0;
+    // The CG's A p vector (read by flexible-CG hooks for beta), given before
+    // the first apply().
+    virtual void bind(const void* ap) { (void)ap; }
     virtual ~ZHook() {}
 };
 

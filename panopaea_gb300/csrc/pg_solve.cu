@@ -389,9 +389,22 @@ int ensure_small(pg_grid* g) {
     return PG_OK;
 }
 
+// One CG run with z from an outer hook (the grid's z buffer; no lazy
+// projection of z's mean).
+static int run_hooked(pg_grid* g, CgConfig cfg, CgBuffers<float> buf, ZHook* hook, pg_pcg_stats* st) {
+    void* z;
+    int rc;
+    if ((rc = extras_of(g)->buffer(Extras::kZ, sizeof(float) * (size_t)g->dims.nc(), &z))) return rc;
+    buf.z = (float*)z;
+    cfg.precond = PG_PRECOND_MG;  // the z-buffer form of the CG kernels
+    cfg.nfluid = 0.0;
+    return run_cg<float>(g, cfg, buf, st, hook);
+}
+
 // Plain CG (the reference algorithm) with library-owned work vectors.
 template <class T>
-static int solve_plain(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, double dt, pg_pcg_stats* st) {
+static int solve_plain(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, double dt, pg_pcg_stats* st,
+                       ZHook* hook = nullptr) {
     Extras* ex = extras_of(g);
     const size_t n = (size_t)g->dims.nc();
     void *r, *ap, *p0, *p1;
@@ -402,13 +415,17 @@ static int solve_plain(pg_grid* g, const pg_solver_params* prm, T* x, const T* b
     CgBuffers<T> buf{x, b, (T*)r, (T*)ap, {(T*)p0, (T*)p1}};
     CgConfig cfg{prm->precond, prm->max_iter, prm->threshold, prm->rel_stop ? prm->rel_tol : 0.0, dt,
                  prm->check_every, 1};
+    if (hook) {
+        if (sizeof(T) != 4) return bad_arg("solver: an outer preconditioner needs f32 fields");
+        return run_hooked(g, cfg, *reinterpret_cast<CgBuffers<float>*>(&buf), hook, st);
+    }
     if (prm->precond == PG_PRECOND_MG) return solve_mgpcg<T>(g, prm, cfg, buf, st);
     return run_cg<T>(g, cfg, buf, st);
 }
 
 // FP32 CG rounds inside FP64 residual refinement.
 static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, const float* b, double dt,
-                         pg_pcg_stats* st) {
+                         pg_pcg_stats* st, ZHook* hook = nullptr) {
     Extras* ex = extras_of(g);
     const i64 n = g->dims.nc();
     int rc;
@@ -484,7 +501,9 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
             }
         }
         pg_pcg_stats s{};
-        if (prm->precond == PG_PRECOND_MG)
+        if (hook)
+            rc = run_hooked(g, cfg, buf, hook, &s);
+        else if (prm->precond == PG_PRECOND_MG)
             rc = solve_mgpcg<float>(g, prm, cfg, buf, &s);
         else
             rc = run_cg<float>(g, cfg, buf, &s);
@@ -542,6 +561,14 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     out.true_residual_max = rmax;
     if (st) *st = out;
     return PG_OK;
+}
+
+int solve_pressure_hooked(pg_grid* g, const pg_solver_params* prm, float* x, const float* b, double dt, ZHook* hook,
+                          pg_pcg_stats* st) {
+    if (prm->max_iter < 0) return bad_arg("solver: max_iter < 0");
+    if (prm->refine > 0) return solve_refined(g, prm, x, b, dt, st, hook);
+    if (prm->initial_guess) return bad_arg("solver: initial_guess needs refine > 0");
+    return solve_plain<float>(g, prm, x, b, dt, st, hook);
 }
 
 template <class T>

@@ -28,4 +28,11 @@ int solve_mgpcg(pg_grid* g, const pg_solver_params* prm, const CgConfig& cfg, Cg
 template <class T>
 int solve_pressure(pg_grid* g, const pg_solver_params* prm, T* x, const T* b, double dt, pg_pcg_stats* st);
 
+// The float pressure solve (plain or in FP64-class refinement, as prm says)
+// with z = M(r) from an outer preconditioner hook whose apply() also folds
+// z.r and beta into the CG state (a flexible CG when M is not linear);
+// prm->precond is not used.
+int solve_pressure_hooked(pg_grid* g, const pg_solver_params* prm, float* x, const float* b, double dt, ZHook* hook,
+                          pg_pcg_stats* st);
+
 }  // namespace pg

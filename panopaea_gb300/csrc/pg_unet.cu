@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "pg_internal.cuh"
+#include "pg_solve.cuh"
 
 namespace pg {
 template <class T> int launch_laplacian(const pg_grid* g, T* out, const T* p, double dt);
@@ -838,6 +839,106 @@ int head(pg_unet* net, const pg_grid* g, double dt, float* p_out, const float* p
     return PG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// The network as a preconditioner correction inside the CG.  For a residual
+// r: q = net(r), a = (q.r) / (q.Aq) (0 when q.Aq <= 0; the step along q that
+// minimises the error's energy norm), then one Jacobi step on what that
+// leaves:
+//     z = M(r) = a q + D^-1 (r - a A q).
+// M is not linear in r (a and the network depend on r), so the CG is the
+// flexible one: beta is the Polak-Ribiere ratio z'.(r' - r) / (z.r), which
+// with r' - r = -alpha A p is -alpha (z'.Ap) / (z.r) -- read from the A p
+// vector the iteration just used, with no copy of the previous residual.
+
+__global__ void k_lp_z(float* __restrict__ z, const float* __restrict__ r, const float* __restrict__ q,
+                       const float* __restrict__ aq, const uint8_t* __restrict__ flags, const float* __restrict__ alpha,
+                       i64 n, float dt, const CgState* st) {
+    if (st->done) return;
+    const float a = *alpha;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (i64)gridDim.x * blockDim.x) {
+        const int open = __popc((unsigned)flags[v] & 63u);
+        const float inv = open ? __frcp_rn((float)open * dt) : 0.f;
+        z[v] = fmaf(a, q[v], (r[v] - a * aq[v]) * inv);
+    }
+}
+
+// z.r and z.Ap (compensated FP32 per thread, FP64 across), then the last
+// block folds them into the CG state: sigma = z.r; after the first
+// iteration beta = -alpha (z.Ap) / sigma_old.
+__global__ void __launch_bounds__(kRedThreads)
+    k_lp_fold(const float* __restrict__ z, const float* __restrict__ r, const float* __restrict__ ap, i64 n,
+              CgState* st, double* partials) {
+    if (st->done) return;
+    __shared__ double sm[32];
+    Acc<float> zr, zap;
+    const bool first = st->iter == 0;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (i64)gridDim.x * blockDim.x) {
+        const float zv = z[v];
+        zr.add(zv * r[v]);
+        if (!first) zap.add(zv * ap[v]);
+    }
+    const double s1 = block_sum<kRedThreads>(zr.value(), sm);
+    const double s2 = block_sum<kRedThreads>(zap.value(), sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = s1;
+        partials[kMaxBlocks + blockIdx.x] = s2;
+    }
+    if (!last_block(&st->counter[3])) return;
+    const double rz = reduce_partials<false, kRedThreads>(partials, gridDim.x, sm);
+    const double za = reduce_partials<false, kRedThreads>(partials + kMaxBlocks, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+        st->counter[3] = 0;
+        if (!isfinite(rz) || !isfinite(za)) {
+            st->status = PG_NAN_DETECTED;
+            st->done = 1;
+        } else if (!(rz > 0.0)) {  // M(r) is not a descent direction for r
+            st->status = PG_BREAKDOWN;
+            st->done = 1;
+        } else if (first) {
+            st->sigma = rz;
+        } else {
+            st->beta = -st->alpha * za / st->sigma;
+            st->sigma = rz;
+            st->first = 0;
+        }
+    }
+}
+
+struct LearnedHook : ZHook {
+    pg_unet* net = nullptr;
+    double dt = 1.0;
+    const float* ap = nullptr;
+    void bind(const void* p) override { ap = (const float*)p; }
+    uintptr_t key() const override { return (uintptr_t)net ^ (uintptr_t)0x9e3779b97f4a7c15ull; }
+    int apply(pg_grid* g, const void* rv, void* zv) override {
+        const float* r = (const float*)rv;
+        float* z = (float*)zv;
+        const i64 V0 = net->lv[0];
+        // the network's kernels run on the CG's stream (a graph capture's)
+        cudaStream_t saved = net->stream;
+        net->stream = g->stream;
+        cudaStream_t s = g->stream;
+        float* alpha = net->scal + 5;
+        int rc = forward(net, g, r, dt);
+        if (!rc) rc = head(net, g, dt, net->q, nullptr);
+        if (!rc) rc = apply_a(net, g, net->ad, net->q, dt);
+        if (!rc) {
+            PG_LAUNCH(KK_UNET_MISC, s, k_dots<<<kRedBlocks, kRedThreads, 0, s>>>(net->q, r, net->ad, V0, net->red));
+            PG_LAUNCH(KK_UNET_MISC, s, k_alpha<<<1, 32, 0, s>>>(net->red, kRedBlocks, alpha));
+            PG_LAUNCH(KK_UNET_MISC, s,
+                      k_lp_z<<<blocks_for(net, V0), 256, 0, s>>>(z, r, net->q, net->ad, g->flags, alpha, V0,
+                                                                 (float)dt, g->ws.state));
+            const int nb = (int)std::min<i64>(kRedBlocks, std::max<i64>(1, (V0 + kRedThreads - 1) / kRedThreads));
+            PG_LAUNCH(KK_UNET_MISC, s,
+                      k_lp_fold<<<nb, kRedThreads, 0, s>>>(z, r, ap, V0, g->ws.state, g->ws.partials));
+            const cudaError_t e = cudaPeekAtLastError();
+            if (e != cudaSuccess) rc = cuda_fail(e, "learned preconditioner launch");
+        }
+        net->stream = saved;
+        return rc;
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -1039,6 +1140,25 @@ int pg_unet_guess_f32(pg_unet* net, const pg_grid* g, const float* b, double dt,
     }
     PG_CHECK_LAUNCH();
     return PG_OK;
+}
+
+
+// z = the learned correction (see LearnedHook) inside a flexible CG, with or
+// without FP64-class refinement as params say.
+int pg_solve_pressure_learned_f32(const pg_grid* g, const pg_solver_params* prm, pg_unet* net, float* x,
+                                  const float* b, double dt, pg_pcg_stats* stats) {
+    if (!g || !prm || !net || !x || !b) return bad_arg("pg_solve_pressure_learned_f32: NULL argument");
+    if (!(dt > 0.0)) return bad_arg("pg_solve_pressure_learned_f32: dt must be > 0");
+    int rc;
+    if ((rc = check_grid(net, g))) return rc;
+    if ((rc = prep_weights(net))) return rc;  // outside any capture of the CG loop
+    LearnedHook hook;
+    hook.net = net;
+    hook.dt = dt;
+    pg_pcg_stats s{};
+    if ((rc = solve_pressure_hooked(const_cast<pg_grid*>(g), prm, x, b, dt, &hook, &s))) return rc;
+    if (stats) *stats = s;
+    return s.status;
 }
 
 }  // extern "C"

@@ -157,6 +157,21 @@ def solve_with_guess(net, grid, x, b, dt, solver, corrections=0):
     return solve_pressure(grid, x, b, dt, cfg)
 
 
+def solve_learned_pcg(net, grid, x, b, dt, solver):
+    """Pressure solve A x = b with the network inside the CG: for a residual
+    r the preconditioner is z = a q + D^-1 (r - a A q), q = net(r), a the
+    energy-optimal step along q (a flexible CG, Polak-Ribiere beta, since z
+    depends on r non-linearly).  The solver's tolerance, refinement and
+    initial_guess apply (its precond does not); returns the statistics."""
+    net._bind_stream()
+    grid._bind_stream()
+    st = N.PcgStats()
+    prm = solver.to_c()
+    grid._call("pg_solve_pressure_learned_f32", C.byref(prm), net._h, _ptr(x.data), _ptr(b.data), C.c_double(dt),
+               C.byref(st), allow=(N.PG_OK, N.PG_NOT_CONVERGED))
+    return st.as_dict()
+
+
 # ---------------------------------------------------------------------------
 # Training data.
 

@@ -154,14 +154,12 @@ def test_bad_shapes(pg):
         net.guess(g, b, 1.0, g.new_simplex_2())
 
 
-def test_trained_network_saves_iterations(pg, oracle):
-    """32^3 grids with 1-6 random boxes and filtered-noise divergence:
-    train (energy-norm loss, 10 epochs) on 384 pairs from the plain solver
-    (FP64-refined CG to relative 1e-6), then solve 8 held-out grids from
-    x = 0 and from the learned guess with the same solver and tolerance.
-    Both runs must meet the tolerance (the network changes the start, never
-    the accuracy); the guess must save >= 5% of the CG iterations, and the
-    guess with one learned correction round >= 10%."""
+@pytest.fixture(scope="module")
+def trained32(pg):
+    """A network trained on 32^3 grids with 1-6 random boxes and
+    filtered-noise divergence (energy-norm loss, 10 epochs, 384 pairs from
+    the plain solver: FP64-refined CG to relative 1e-6), and 8 held-out
+    grids."""
     from panopaea_gb300 import learned
 
     dims = (32, 32, 32)
@@ -172,6 +170,18 @@ def test_trained_network_saves_iterations(pg, oracle):
     scale = learned.estimate_out_scale(pairs, 1.0)
     net = learned.PressureNet(dims, out_scale=scale, seed=1)
     hist = learned.train(net, g, pairs, 1.0, epochs=10, batch=4, lr=1e-3)
+    return g, net, held, hist
+
+
+def test_trained_network_saves_iterations(pg, oracle, trained32):
+    """Solve the 8 held-out grids from x = 0 and from the learned guess with
+    the same solver and tolerance.  Both runs must meet the tolerance (the
+    network changes the start, never the accuracy); the guess must save
+    >= 5% of the CG iterations, and the guess with one learned correction
+    round >= 10%."""
+    from panopaea_gb300 import learned
+
+    g, net, held, hist = trained32
     assert hist[-1] < 0.2 * hist[0]
     solver = pg.SolverConfig(rel_stop=True, rel_tol=1e-6, max_iter=20000, refine=8)
     it = {0: [], 1: [], 2: []}
@@ -188,3 +198,37 @@ def test_trained_network_saves_iterations(pg, oracle):
     print("CG iterations from zero %s, learned guess %s, guess + 1 correction %s" % (it[0], it[1], it[2]))
     assert np.mean(it[1]) <= 0.95 * np.mean(it[0])
     assert np.mean(it[2]) <= 0.90 * np.mean(it[0])
+
+
+def test_learned_preconditioner_inside_cg(pg, oracle, trained32):
+    """The trained network as a preconditioner correction inside the CG
+    (flexible CG, z = a net(r) + D^-1 (r - a A net(r))) on the held-out
+    grids, in FP64-class refinement to relative 1e-6: every solve meets the
+    tolerance (checked in FP64 by the oracle's operator), and it needs fewer
+    iterations than plain CG and than Jacobi-PCG on the same grids."""
+    from panopaea_gb300 import learned
+
+    g, net, held, _ = trained32
+    dims = (32, 32, 32)
+    its = {"plain": [], "jacobi": [], "learned": []}
+    for b, _, mask in held:
+        g.set_solid_cells(mask)
+        fs = oracle.cell_mask_to_faces(mask)
+        for name, precond in (("plain", 0), ("jacobi", 1)):
+            x = g.new_simplex_2()
+            st = pg.solve_pressure(g, x, b, 1.0, pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=1e-6,
+                                                                 max_iter=20000, refine=8))
+            assert st["status"] == 0
+            its[name].append(st["iterations"])
+        x = g.new_simplex_2()
+        st = learned.solve_learned_pcg(net, g, x, b, 1.0, pg.SolverConfig(rel_stop=True, rel_tol=1e-6,
+                                                                          max_iter=20000, refine=8))
+        assert st["status"] == 0 and st["true_residual_max"] <= 1e-6 * st["b_max"], st
+        bh = host(b).astype(np.float64)
+        true_r = np.abs(bh - oracle.laplacian(host(x).astype(np.float64), 1.0, dims, fs)).max()
+        assert true_r <= 1e-5 * np.abs(bh).max()  # x returned in FP32
+        its["learned"].append(st["iterations"])
+    print("iterations: plain CG %s, Jacobi-PCG %s, learned preconditioner (flexible CG) %s" %
+          (its["plain"], its["jacobi"], its["learned"]))
+    assert np.mean(its["learned"]) < np.mean(its["jacobi"])
+    assert np.mean(its["learned"]) < np.mean(its["plain"])
