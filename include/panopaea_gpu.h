@@ -453,6 +453,10 @@ int pg_unet_guess_f32(pg_unet* net, const pg_grid* grid, const float* b, double 
  * Synchronous; returns the solve's status. */
 int pg_solve_pressure_learned_f32(const pg_grid* grid, const pg_solver_params* params, pg_unet* net, float* x,
                                   const float* b, double dt, pg_pcg_stats* stats);
+/* Waits for the network's stream; PG_TIMEOUT if one of its tensor-core
+ * kernels gave up a bounded wait since the last check (its results are then
+ * not to be trusted; the flag is cleared), else PG_OK. */
+int pg_unet_check(pg_unet* net);
 
 /* ----------------------------------------------------------------------- */
 /* Instrumentation (no reference counterpart; the reference only prints

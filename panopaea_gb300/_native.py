@@ -149,6 +149,7 @@ _SIGS = {
     "pg_unet_accumulate_f32": (_I, [_P, _P, _P, _P, _D, C.POINTER(_D)]),
     "pg_unet_adam_step": (_I, [_P, C.POINTER(AdamParams)]),
     "pg_unet_guess_f32": (_I, [_P, _P, _P, _D, _I, _P]),
+    "pg_unet_check": (_I, [_P]),
     "pg_solve_pressure_learned_f32": (_I, [_P, C.POINTER(SolverParams), _P, _P, _P, _D, C.POINTER(PcgStats)]),
     "pg_unet_forward_f32": (_I, [_P, _P, _P, _D, _P]),
     "pg_unet_set_loss": (_I, [_P, _I]),

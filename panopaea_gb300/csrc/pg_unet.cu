@@ -39,6 +39,7 @@
 
 #include "pg_internal.cuh"
 #include "pg_solve.cuh"
+#include "pg_tma.cuh"
 
 namespace pg {
 template <class T> int launch_laplacian(const pg_grid* g, T* out, const T* p, double dt);
@@ -197,6 +198,254 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(const bf16* __restrict__ 
             }
         }
 }
+
+// ---------------------------------------------------------------------------
+// The same convolution on the fifth-generation tensor cores: tcgen05.mma
+// (kind::f16, BF16 operands, FP32 accumulators in tensor memory), issued by
+// one thread, operands described in shared memory.
+//
+// GEMM per CTA: M = 128 output voxels (an 8 x 16 x-y tile of one z plane),
+// N = C_out, K = 27 taps x C_in; TZ consecutive z planes per CTA, each with
+// its own 128 x N accumulator in tensor memory.  The input brick (tile plus
+// a one-voxel halo, TZ + 2 planes) is staged per 16-channel chunk in a
+// chunk-planar layout: [8-channel half][bz][by][bx] x 16 bytes.  In that
+// layout the A operand of every tap is a plain K-major, no-swizzle operand
+// inside the brick -- core matrices of 8 consecutive x voxels x 16 bytes
+// (contiguous 128 B), 8-row groups one brick row (BX x 16 B) apart, the two
+// 8-channel halves one plane apart -- so a tap is only a different start
+// address: no im2col copy.  The weights of a chunk arrive pre-laid-out as
+// [tap][8-channel half][n][8] (B operand, K-major: n rows 16 B apart, 8-row
+// groups 128 B apart, halves N x 16 B apart).
+namespace tc {
+
+constexpr int TX = 8, TY = 16, BX = TX + 2, BY = TY + 2;
+constexpr int kThreads = 256;
+
+// Shared-memory matrix descriptor, no swizzle (start, leading- and
+// stride-dimension byte offsets in 16-byte units; descriptor version 1).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+// One arrival on bar once every tcgen05.mma this thread issued has completed.
+__device__ __forceinline__ void commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 8 consecutive 32-bit columns of this thread's lane.
+__device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int COUT> struct Cfg {
+    static constexpr int TZ = COUT >= 96 ? 2 : 4;
+    static constexpr int BZ = TZ + 2;
+    static constexpr int kPlane = BX * BY * BZ * 16;      // one 8-channel half of the brick
+    static constexpr int kBrick = 2 * kPlane;             // one 16-channel chunk
+    static constexpr int kWTap = 2 * COUT * 16;           // one tap of one chunk
+    static constexpr int kWChunk = 27 * kWTap;
+    static constexpr int kBrickOff = 128, kWOff = kBrickOff + kBrick;
+    static constexpr size_t kSmem = 128 + (size_t)kBrick + kWChunk;
+    static constexpr int kCols = TZ * COUT <= 32 ? 32 : (TZ * COUT <= 64 ? 64 : (TZ * COUT <= 128 ? 128 : (TZ * COUT <= 256 ? 256 : 512)));
+    static_assert(TZ * COUT <= 512, "accumulators must fit in tensor memory");
+    static_assert(kPlane % 16 == 0 && kBrick % 128 == 0, "operand alignment");
+};
+
+struct Geom {
+    int D, H, W;
+    int tiles_x, tiles_y;
+};
+
+// wtc: [chunk][tap][half][n][8] BF16 (see above); err: set when a wait for
+// the tensor cores gave up (the result is then not to be trusted).
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads) k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wtc,
+                                                      bf16* __restrict__ out, const bf16* __restrict__ gate, Geom G,
+                                                      int epi, int* err) {
+    typedef Cfg<COUT> C;
+    constexpr int KC = CIN / 16, TZ = C::TZ;
+    constexpr uint32_t kIdesc = idesc_bf16(128, COUT);
+    extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    unsigned char* const base = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
+    uint64_t* const bar = (uint64_t*)base;
+    uint32_t* const tslot = (uint32_t*)(base + 8);
+    unsigned char* const brick = base + C::kBrickOff;
+    unsigned char* const wsm = base + C::kWOff;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int t = blockIdx.x;
+    const int x0 = (t % G.tiles_x) * TX;
+    t /= G.tiles_x;
+    const int y0 = (t % G.tiles_y) * TY;
+    const int z0 = (t / G.tiles_y) * TZ;
+    if (warp == 0) tmem_alloc(tslot, C::kCols);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    bool ok = true;  // block-uniform
+    int committed = -1;
+    for (int kc = 0; kc < KC; ++kc) {
+        if (kc > 0) {  // the previous chunk's MMAs have read the brick and the weights
+            bool w = true;
+            if (tid == 0) w = mbar_wait(bar, (kc - 1) & 1);
+            ok = !__syncthreads_or(!w);
+            if (!ok) break;
+        }
+        // brick of this chunk: voxel (bx, by, bz) half hf at brick + hf * plane + voxel * 16
+        constexpr int nvox = BX * BY * C::BZ;
+        for (int i = tid; i < 2 * nvox; i += kThreads) {
+            const int hf = i & 1, v = i >> 1;
+            const int bx = v % BX, r = v / BX, by = r % BY, bz = r / BY;
+            const int gx = x0 + bx - 1, gy = y0 + by - 1, gz = z0 + bz - 1;
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if ((unsigned)gx < (unsigned)G.W && (unsigned)gy < (unsigned)G.H && (unsigned)gz < (unsigned)G.D)
+                val = __ldg(reinterpret_cast<const uint4*>(in + (((size_t)gz * G.H + gy) * G.W + gx) * CIN + kc * 16 +
+                                                           hf * 8));
+            *reinterpret_cast<uint4*>(brick + hf * C::kPlane + v * 16) = val;
+        }
+        // weights of this chunk (contiguous)
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(wtc + (size_t)kc * (C::kWChunk / 2));
+            uint4* dst = reinterpret_cast<uint4*>(wsm);
+            for (int i = tid; i < C::kWChunk / 16; i += kThreads) dst[i] = __ldg(src + i);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor-core reads
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            const uint32_t bs = smem_u32(brick), ws = smem_u32(wsm);
+#pragma unroll 1
+            for (int tap = 0; tap < 27; ++tap) {
+                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                const uint64_t bdesc = sdesc(ws + tap * C::kWTap, COUT * 16, 128);
+#pragma unroll
+                for (int tz = 0; tz < TZ; ++tz) {
+                    const uint32_t a = bs + (uint32_t)((((tz + dz) * BY + dy) * BX + dx) * 16);
+                    mma(tmem + (uint32_t)(tz * COUT), sdesc(a, C::kPlane, BX * 16), bdesc, kIdesc,
+                        (kc > 0 || tap > 0) ? 1u : 0u);
+                }
+            }
+            commit(bar);
+        }
+        committed = kc;
+    }
+    // every MMA has completed before the accumulators are read
+    if (ok) {
+        bool w = true;
+        if (tid == 0) w = mbar_wait(bar, (KC - 1) & 1);
+        ok = !__syncthreads_or(!w);
+    }
+    if (!ok) {
+        // a wait gave up: flag it, wait once more (bounded) for the tensor
+        // cores' last committed group, and leave the accumulators unread
+        if (tid == 0) {
+            atomicExch(err, 1);
+            if (committed >= 0) mbar_wait(bar, committed & 1);
+        }
+        __syncthreads();
+    } else {
+        fence_after();
+        // warp w reads lanes 32 (w % 4) .. +31 (rows of the tile) of the planes of its half
+        const int q = warp & 3, half = warp >> 2;
+        const int m = q * 32 + lane;
+        const int x = x0 + (m & 7), y = y0 + (m >> 3);
+        constexpr int PZ = TZ / 2;
+#pragma unroll 1
+        for (int tz = half * PZ; tz < (half + 1) * PZ; ++tz) {
+            const int z = z0 + tz;
+            const bool in_grid = x < G.W && y < G.H && z < G.D;
+            const size_t o = (((size_t)z * G.H + y) * G.W + x) * COUT;
+#pragma unroll 1
+            for (int cg = 0; cg < COUT / 8; ++cg) {
+                float v[8];
+                ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(tz * COUT + cg * 8), v);
+                if (!in_grid) continue;
+                if (epi == EPI_RELU) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) v[i] = v[i] > 0.f ? v[i] : 0.f;
+                } else if (epi == EPI_GATE) {
+                    const uint4 gv = *reinterpret_cast<const uint4*>(gate + o + cg * 8);
+                    const uint32_t gw[4] = {gv.x, gv.y, gv.z, gv.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        __nv_bfloat162 pr;
+                        memcpy(&pr, &gw[i], 4);
+                        if (!(__bfloat162float(pr.x) > 0.f)) v[2 * i] = 0.f;
+                        if (!(__bfloat162float(pr.y) > 0.f)) v[2 * i + 1] = 0.f;
+                    }
+                }
+                *reinterpret_cast<uint4*>(out + o + cg * 8) =
+                    make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                               pack_bf16(v[6], v[7]));
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc(tmem, C::kCols);
+    }
+}
+
+// Weights of the tensor-core path: wtc[chunk][tap][half][n][8] with the
+// K index k = 16 chunk + 8 half + j an input channel of the convolution and
+// n an output channel; forward W[tap][k][n], backward-data (transposed,
+// tap-mirrored) W[26 - tap][n][k] of the forward layer.
+__global__ void k_wprep_tc(const float* __restrict__ W, int cin, int cout, int transposed, bf16* __restrict__ wtc) {
+    const int K = transposed ? cout : cin, N = transposed ? cin : cout;
+    const int n_all = 27 * K * N;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_all; i += gridDim.x * blockDim.x) {
+        const int j = i & 7;
+        int r = i >> 3;
+        const int n = r % N;
+        r /= N;
+        const int hf = r & 1;
+        r >>= 1;
+        const int tap = r % 27, kc = r / 27;
+        const int k = kc * 16 + hf * 8 + j;
+        const float v = transposed ? W[((size_t)(26 - tap) * cin + n) * cout + k] : W[((size_t)tap * cin + k) * cout + n];
+        wtc[i] = __float2bfloat16_rn(v);
+    }
+}
+
+}  // namespace tc
 
 // ---------------------------------------------------------------------------
 // Weight gradient: part[slab][tap][ci][co] = sum over the slab's voxels v of
@@ -618,6 +867,9 @@ struct pg_unet {
     float* adam_v = nullptr;
     uint2* wf[kL] = {};
     uint2* wt[kL] = {};
+    bf16* tcf[kL] = {};  // tensor-core (tcgen05) weight layouts: forward
+    bf16* tct[kL] = {};  // and backward-data
+    int* err = nullptr;  // set by a kernel whose bounded wait gave up
     bool wdirty = true;
     bf16 *X0 = nullptr, *Y[kL] = {}, *P0 = nullptr, *P1 = nullptr, *C1 = nullptr, *C0 = nullptr;
     bf16 *G0a = nullptr, *G0b = nullptr, *dC0 = nullptr, *G1a = nullptr, *G1b = nullptr, *dC1 = nullptr,
@@ -682,8 +934,66 @@ int conv_t(const pg_unet* net, int lvl, const bf16* in, const uint2* w, bf16* ou
     return PG_OK;
 }
 
-int conv(const pg_unet* net, int lvl, int cin, int cout, const bf16* in, const uint2* w, bf16* out, const bf16* gate,
-         int epi) {
+// The tensor-core convolution: one CTA per 8 x 16 x TZ output tile; the
+// launch's dynamic shared memory also caps the CTAs per SM so that their
+// tensor-memory columns fit in the SM's 512.
+template <int CIN, int COUT>
+int conv_tc_t(const pg_unet* net, int lvl, const bf16* in, const bf16* wtc, bf16* out, const bf16* gate, int epi) {
+    typedef tc::Cfg<COUT> Cf;
+    static size_t smem = 0;
+    if (!smem) {
+        size_t s = Cf::kSmem + 128;
+        PG_CUDA(cudaFuncSetAttribute(tc::k_conv_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     227 * 1024));
+        const int maxb = 512 / Cf::kCols;
+        int bps = 0;
+        PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, tc::k_conv_tc<CIN, COUT>, tc::kThreads, s));
+        if (bps > maxb) {
+            s = std::max(s, (size_t)(228 * 1024 / (maxb + 1) - 1024 + 128));
+            PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, tc::k_conv_tc<CIN, COUT>, tc::kThreads, s));
+        }
+        if (bps < 1 || bps > maxb) return bad_arg("pg_unet: tensor-core conv does not fit an SM");
+        smem = s;
+    }
+    tc::Geom G;
+    G.D = net->ld[lvl];
+    G.H = net->lh[lvl];
+    G.W = net->lw[lvl];
+    G.tiles_x = ceil_div(G.W, tc::TX);
+    G.tiles_y = ceil_div(G.H, tc::TY);
+    const int nb = G.tiles_x * G.tiles_y * ceil_div(G.D, Cf::TZ);
+    PG_LAUNCH(KK_UNET_CONV, net->stream,
+              tc::k_conv_tc<CIN, COUT><<<nb, tc::kThreads, smem, net->stream>>>(in, wtc, out, gate, G, epi, net->err));
+    PG_CHECK_LAUNCH();
+    return PG_OK;
+}
+
+// The tensor-core path unless PG_UNET_TC=0 (a diagnostic switch: the legacy
+// warp-level mma.sync kernel, kept for comparison).
+bool tc_enabled() {
+    const char* env = getenv("PG_UNET_TC");
+    return !(env && env[0] == '0');
+}
+
+int conv(const pg_unet* net, int lvl, int cin, int cout, const bf16* in, const uint2* w, const bf16* wtc, bf16* out,
+         const bf16* gate, int epi) {
+    if (tc_enabled()) {
+#define PG_UNET_CONV_TC(A, B) \
+    if (cin == A && cout == B) return conv_tc_t<A, B>(net, lvl, in, wtc, out, gate, epi);
+        PG_UNET_CONV_TC(16, 16)
+        PG_UNET_CONV_TC(16, 32)
+        PG_UNET_CONV_TC(32, 32)
+        PG_UNET_CONV_TC(32, 64)
+        PG_UNET_CONV_TC(64, 64)
+        PG_UNET_CONV_TC(96, 32)
+        PG_UNET_CONV_TC(48, 16)
+        PG_UNET_CONV_TC(16, 48)
+        PG_UNET_CONV_TC(32, 96)
+        PG_UNET_CONV_TC(64, 32)
+        PG_UNET_CONV_TC(32, 16)
+#undef PG_UNET_CONV_TC
+        return bad_arg("pg_unet: no conv kernel for this channel pair");
+    }
 #define PG_UNET_CONV(A, B) \
     if (cin == A && cout == B) return conv_t<A, B>(net, lvl, in, w, out, gate, epi);
     PG_UNET_CONV(16, 16)
@@ -738,10 +1048,29 @@ int prep_weights(pg_unet* net) {
         PG_LAUNCH(KK_UNET_MISC, net->stream,
                   k_wprep<<<ceil_div(n, 256), 256, 0, net->stream>>>(net->params + param_offset(k), kCin[k], kCout[k],
                                                                       net->wf[k], k ? net->wt[k] : nullptr));
+        const int nt = 27 * kCin[k] * kCout[k];
+        PG_LAUNCH(KK_UNET_MISC, net->stream,
+                  tc::k_wprep_tc<<<ceil_div(nt, 256), 256, 0, net->stream>>>(net->params + param_offset(k), kCin[k],
+                                                                              kCout[k], 0, net->tcf[k]));
+        if (k)
+            PG_LAUNCH(KK_UNET_MISC, net->stream,
+                      tc::k_wprep_tc<<<ceil_div(nt, 256), 256, 0, net->stream>>>(net->params + param_offset(k), kCin[k],
+                                                                                  kCout[k], 1, net->tct[k]));
     }
     PG_CHECK_LAUNCH();
     net->wdirty = false;
     return PG_OK;
+}
+
+// PG_TIMEOUT (and the flag cleared) when a tensor-core wait gave up since
+// the last check; synchronous.
+int check_err(pg_unet* net) {
+    int e = 0;
+    PG_CUDA(cudaMemcpy(&e, net->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!e) return PG_OK;
+    PG_CUDA(cudaMemset(net->err, 0, sizeof(int)));
+    set_error("pg_unet: a wait for the tensor cores gave up; the network's last results are not to be trusted");
+    return PG_TIMEOUT;
 }
 
 int check_grid(const pg_unet* net, const pg_grid* g) {
@@ -761,7 +1090,9 @@ int forward(pg_unet* net, const pg_grid* g, const float* b, double dt) {
     PG_LAUNCH(KK_UNET_MISC, s, k_scalars<<<1, 32, 0, s>>>(net->red, kRedBlocks, V0, (float)net->out_scale, (float)dt, net->scal));
     PG_LAUNCH(KK_UNET_MISC, s, k_input<<<blocks_for(net, V0), 256, 0, s>>>(b, g->flags, net->scal, V0, net->X0));
     PG_CHECK_LAUNCH();
-    auto C = [&](int k, const bf16* in) { return conv(net, kLevel[k], kCin[k], kCout[k], in, net->wf[k], net->Y[k], nullptr, EPI_RELU); };
+    auto C = [&](int k, const bf16* in) {
+        return conv(net, kLevel[k], kCin[k], kCout[k], in, net->wf[k], net->tcf[k], net->Y[k], nullptr, EPI_RELU);
+    };
     if ((rc = C(0, net->X0)) || (rc = C(1, net->Y[0]))) return rc;
     PG_LAUNCH(KK_UNET_MISC, s, k_pool<<<blocks_for(net, net->lv[1] * 16), 256, 0, s>>>(net->Y[1], 16, net->ld[0], net->lh[0], net->lw[0], net->P0));
     if ((rc = C(2, net->P0)) || (rc = C(3, net->Y[2]))) return rc;
@@ -781,7 +1112,7 @@ int backward(pg_unet* net) {
     const int d0 = net->ld[0], h0 = net->lh[0], w0 = net->lw[0];
     const int d1 = net->ld[1], h1 = net->lh[1], w1 = net->lw[1];
     auto BD = [&](int k, const bf16* dz, bf16* out, const bf16* gate, int epi) {
-        return conv(net, kLevel[k], kCout[k], kCin[k], dz, net->wt[k], out, gate, epi);
+        return conv(net, kLevel[k], kCout[k], kCin[k], dz, net->wt[k], net->tct[k], out, gate, epi);
     };
     // level 0 decoder: dZ9 = G0a (from k_head)
     if ((rc = wgrad(net, 9, net->Y[8], net->G0a)) || (rc = BD(9, net->G0a, net->G0b, net->Y[8], EPI_GATE))) return rc;
@@ -978,7 +1309,10 @@ int pg_unet_create(int64_t d, int64_t h, int64_t w, pg_unet** out) {
     for (int k = 0; k < kL; ++k) {
         add((void**)&net->wf[k], 8 * (size_t)27 * kCin[k] * kCout[k] / 4);
         if (k) add((void**)&net->wt[k], 8 * (size_t)27 * kCin[k] * kCout[k] / 4);
+        add((void**)&net->tcf[k], 2 * (size_t)27 * kCin[k] * kCout[k]);
+        if (k) add((void**)&net->tct[k], 2 * (size_t)27 * kCin[k] * kCout[k]);
     }
+    add((void**)&net->err, sizeof(int));
     const i64 V0 = net->lv[0], V1 = net->lv[1], V2 = net->lv[2];
     add((void**)&net->X0, 2 * V0 * 16);
     for (int k = 0; k < kL; ++k) add((void**)&net->Y[k], 2 * (size_t)net->lv[kLevel[k]] * kCout[k]);
@@ -1082,8 +1416,15 @@ int pg_unet_accumulate_f32(pg_unet* net, const pg_grid* g, const float* b, const
     if (loss) {
         PG_CUDA(cudaMemcpyAsync(loss, net->loss, sizeof(double), cudaMemcpyDeviceToHost, net->stream));
         PG_CUDA(cudaStreamSynchronize(net->stream));
+        return check_err(net);
     }
     return PG_OK;
+}
+
+int pg_unet_check(pg_unet* net) {
+    if (!net) return bad_arg("pg_unet_check: NULL network");
+    PG_CUDA(cudaStreamSynchronize(net->stream));
+    return check_err(net);
 }
 
 int pg_unet_adam_step(pg_unet* net, const pg_adam_params* a) {
@@ -1157,6 +1498,7 @@ int pg_solve_pressure_learned_f32(const pg_grid* g, const pg_solver_params* prm,
     hook.dt = dt;
     pg_pcg_stats s{};
     if ((rc = solve_pressure_hooked(const_cast<pg_grid*>(g), prm, x, b, dt, &hook, &s))) return rc;
+    if ((rc = check_err(net))) return rc;
     if (stats) *stats = s;
     return s.status;
 }

@@ -232,3 +232,35 @@ def test_learned_preconditioner_inside_cg(pg, oracle, trained32):
           (its["plain"], its["jacobi"], its["learned"]))
     assert np.mean(its["learned"]) < np.mean(its["jacobi"])
     assert np.mean(its["learned"]) < np.mean(its["plain"])
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (32, 48, 40)])
+def test_tensor_core_convs_equal_warp_mma(pg, oracle, dims, monkeypatch):
+    """The convolutions on the fifth-generation tensor cores (tcgen05.mma,
+    FP32 accumulators in tensor memory) against the warp-level mma.sync
+    kernel (PG_UNET_TC=0): the same forward output and loss and every
+    layer's weight gradient, to the BF16 storage rounding the two FP32
+    summation orders can flip (the bounds of the oracle comparison: output
+    1% and loss 1e-3, gradients 8% relative L2 with cosine >= 0.99); no
+    tensor-core wait gave up."""
+    from panopaea_gb300 import _native as N
+    from panopaea_gb300 import learned
+
+    g, mask, fs, b, pt, params = _case(pg, oracle, dims, seed=61 + dims[1])
+    gb, gpt = pg.Simplex2(g, dev(b)), pg.Simplex2(g, dev(pt))
+    res = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("PG_UNET_TC", tc)
+        net = learned.PressureNet(dims, params=params, out_scale=3.0)
+        x = g.new_simplex_2()
+        net.forward(g, gb, 0.5, x)
+        loss = net.accumulate(g, gb, gpt, 0.5)
+        assert N.load().pg_unet_check(net._h) == N.PG_OK
+        res[tc] = (host(x), loss, net.get_grads())
+    (x1, l1, g1), (x0, l0, g0) = res["1"], res["0"]
+    assert np.linalg.norm(x1 - x0) <= 1e-2 * np.linalg.norm(x0)
+    assert abs(l1 - l0) <= 1e-3 * l0
+    for k in range(10):
+        a, c = g1[OFFS[k]:OFFS[k + 1]], g0[OFFS[k]:OFFS[k + 1]]
+        assert np.linalg.norm(a - c) <= 8e-2 * np.linalg.norm(c), (k, np.linalg.norm(a - c) / np.linalg.norm(c))
+        assert np.vdot(a, c) >= 0.99 * np.linalg.norm(a) * np.linalg.norm(c), k
