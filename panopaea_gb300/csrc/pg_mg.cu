@@ -66,14 +66,16 @@ struct MgHierarchy {
     float* e0b = nullptr;
     CUtensorMap gmap;  // level-0 flags
     CUtensorMap cmap;  // level-1 correction (prolongation)
+    CUtensorMap rgmap;  // level-0 flags, the restriction's tile box
+    bool restrict_tma = false;  // fine restriction by k_mg_restrict3p (3D, even sides)
     int pair_cap = 0;          // resident k_mg_pair blocks on the device (every mode)
     int pair_cap_plain = 0;    // the same for the modes without the coarse correction
     struct MapEnt {
         const void* p = nullptr;
-        int by = 0;
+        int bx = 0, by = 0;
         CUtensorMap m;
     };
-    mutable MapEnt maps[6];
+    mutable MapEnt maps[8];
     mutable int next_map = 0;
 };
 
@@ -459,6 +461,158 @@ __global__ void __launch_bounds__(kPThreads, kPMinBlocks)
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Fine-level restriction of 3D grids with even sides, TMA-staged: a block
+// owns a kQX x kQY tile of fine cells (kQX/2 x kQY/2 coarse cells, one per
+// thread) and walks a range of coarse planes (ZWalk over the coarse tile
+// columns); fine plane p is staged with e (one-cell halo), f and the flags
+// into a kQStages-deep ring, and coarse plane Z reads the stages of fine
+// planes 2Z-1 .. 2Z+2.  Each thread sums its eight children's residuals
+// f - A e in the order and with the arithmetic of k_mg_restrict<true>
+// (bit-identical).  Per fine cell: 4 bytes of e (+ halo), 4 of f, 1 of flags
+// in; 0.5 of the coarse right-hand side out.
+constexpr int kQX = 64, kQY = 16, kQThreads = (kQX / 2) * (kQY / 2);
+constexpr int kQStages = 6;
+constexpr int kQEw = kQX + 8, kQEh = kQY + 2;  // e box from (x0 - 4, y0 - 1)
+constexpr int kQEBytes = kQEw * kQEh * 4, kQFBytes = kQX * kQY * 4, kQGBytes = kQX * kQY;
+constexpr int kQFOff = ((kQEBytes + 127) / 128) * 128, kQGOff = kQFOff + kQFBytes;
+constexpr int kQStageBytes = kQGOff + ((kQGBytes + 127) / 128) * 128;
+constexpr int kQBarOff = kQStages * kQStageBytes;
+constexpr size_t kQSmem = 128 + kQBarOff + kQStages * 8;
+constexpr unsigned kQTx = kQEBytes + kQFBytes + kQGBytes;
+static_assert(kQStageBytes % 128 == 0 && kQFOff % 128 == 0 && kQGOff % 128 == 0, "TMA boxes 128-byte aligned");
+
+struct RestrictArgs {
+    int d, h, w;  // fine
+    int ch, cw;   // coarse rows and columns
+    float dt;
+    float* fc;
+    int tiles_x, tiles_y;
+};
+
+__global__ void __launch_bounds__(kQThreads)
+    k_mg_restrict3p(const __grid_constant__ CUtensorMap emap, const __grid_constant__ CUtensorMap fmap,
+                    const __grid_constant__ CUtensorMap gmap, RestrictArgs a, CgState* st) {
+    if (st->done) return;
+    extern __shared__ unsigned char rs_smem_raw[];
+    unsigned char* const base = rs_smem_raw + ((128u - (smem_u32(rs_smem_raw) & 127u)) & 127u);
+    uint64_t* const bars = (uint64_t*)(base + kQBarOff);
+    const int tid = threadIdx.x, cx = tid % (kQX / 2), cy = tid / (kQX / 2);
+    if (tid == 0) {
+        for (int s = 0; s < kQStages; ++s) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+        tma_prefetch_map(&emap);
+        tma_prefetch_map(&fmap);
+        tma_prefetch_map(&gmap);
+    }
+    __syncthreads();
+    const float dt = a.dt;
+    const int d = a.d;
+    auto stage = [&](unsigned j) -> const unsigned char* { return base + (j % kQStages) * kQStageBytes; };
+    unsigned issued_end = 0;
+    auto issue = [&](unsigned j, int plane, int x0, int y0) {
+        issued_end = j + 1;
+        unsigned char* dst = base + (j % kQStages) * kQStageBytes;
+        uint64_t* bar = &bars[j % kQStages];
+        mbar_expect_tx(bar, kQTx);
+        tma_load_3d(dst, &emap, bar, x0 - 4, y0 - 1, plane);
+        tma_load_3d(dst + kQFOff, &fmap, bar, x0, y0, plane);
+        tma_load_3d(dst + kQGOff, &gmap, bar, x0, y0, plane);
+    };
+    bool ok = true;
+    auto wait = [&](unsigned j) {
+        if (tid == 0 && ok) ok = mbar_wait(&bars[j % kQStages], (j / kQStages) & 1);
+    };
+    unsigned seq = 0;
+    bool failed = false;
+    const int cd = d / 2;
+    ZWalk walk(a.tiles_x * a.tiles_y, cd);
+    int t2, Z0, Z1;
+    while (!failed && walk.next(t2, Z0, Z1)) {
+        const int x0 = (t2 % a.tiles_x) * kQX, y0 = (t2 / a.tiles_x) * kQY;
+        const int n = 2 * (Z1 - Z0) + 2;  // fine planes 2 Z0 - 1 .. 2 Z1 (ring index j = plane - 2 Z0 + 1)
+        if (tid == 0)
+            for (int j = 0; j < min(n, kQStages); ++j) issue(seq + j, 2 * Z0 - 1 + j, x0, y0);
+        for (int i = 0; i < Z1 - Z0; ++i) {
+            // coarse plane Z0 + i reads ring entries 2i .. 2i + 3
+            if (i == 0) {
+                wait(seq);
+                wait(seq + 1);
+            }
+            wait(seq + 2 * i + 2);
+            wait(seq + 2 * i + 3);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            float sum = 0.f;
+#pragma unroll
+            for (int dz = 0; dz < 2; ++dz) {
+                const unsigned char *Pm = stage(seq + 2 * i + dz), *P0 = stage(seq + 2 * i + dz + 1),
+                                    *Pp = stage(seq + 2 * i + dz + 2);
+                const float* E0 = (const float*)P0;
+                const float* Em = (const float*)Pm;
+                const float* Ep = (const float*)Pp;
+                const float* F0 = (const float*)(P0 + kQFOff);
+                const unsigned char* G0 = P0 + kQGOff;
+#pragma unroll
+                for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                    for (int dx = 0; dx < 2; ++dx) {
+                        const int yl = 2 * cy + dy, xl = 2 * cx + dx;
+                        const int ei = (yl + 1) * kQEw + xl + 4;
+                        const unsigned fl = G0[yl * kQX + xl];
+                        const float ecv = E0[ei];
+                        float acc = 0.f;
+                        if (fl & XLO) acc = fmaf(dt, ecv - E0[ei - 1], acc);
+                        if (fl & XHI) acc = fmaf(dt, ecv - E0[ei + 1], acc);
+                        if (fl & YLO) acc = fmaf(dt, ecv - E0[ei - kQEw], acc);
+                        if (fl & YHI) acc = fmaf(dt, ecv - E0[ei + kQEw], acc);
+                        if (fl & ZLO) acc = fmaf(dt, ecv - Em[ei], acc);
+                        if (fl & ZHI) acc = fmaf(dt, ecv - Ep[ei], acc);
+                        sum += F0[yl * kQX + xl] - acc;
+                    }
+            }
+            const int X = x0 / 2 + cx, Y = y0 / 2 + cy;
+            if (X < a.cw && Y < a.ch) a.fc[((i64)(Z0 + i) * a.ch + Y) * a.cw + X] = sum;
+            __syncthreads();  // ring entries 2i, 2i + 1 are free: refill them
+            if (tid == 0) {
+                if (2 * i + kQStages < n) issue(seq + 2 * i + kQStages, 2 * Z0 - 1 + 2 * i + kQStages, x0, y0);
+                if (2 * i + 1 + kQStages < n) issue(seq + 2 * i + 1 + kQStages, 2 * Z0 + 2 * i + kQStages, x0, y0);
+            }
+        }
+        if (failed) break;
+        __syncthreads();
+        seq += n;
+    }
+    if (failed) {  // a plane never arrived: drain the copies in flight (bounded), stop the solve
+        if (tid == 0) {
+            const uint64_t t0 = global_ns();
+            for (unsigned j = issued_end > kQStages ? issued_end - kQStages : 0; j < issued_end; ++j)
+                while (!mbar_try_wait(&bars[j % kQStages], (j / kQStages) & 1) && global_ns() - t0 < kMbarWaitNs) {
+                }
+            st->status = PG_TIMEOUT;
+            st->done = 1;
+        }
+    }
+}
+
+static int restrict_cap(const pg_grid* g) {
+    static int cap = -1;
+    if (cap < 0) {
+        cap = 0;
+        if (cudaFuncSetAttribute(k_mg_restrict3p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQSmem) ==
+            cudaSuccess) {
+            int bps = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_mg_restrict3p, kQThreads, kQSmem) ==
+                cudaSuccess)
+                cap = std::min(bps * g->num_sms, kMaxBlocks);
+        }
+        cudaGetLastError();
+    }
+    return cap;
 }
 
 // Residual of level l restricted (summed over children) to level l+1.
@@ -940,19 +1094,26 @@ static int pair_setup(pg_grid* g, MgHierarchy* H) {
     H->pair_cap = std::min(std::min(plain, std::min(bps[3], bps[4])) * g->num_sms, kMaxBlocks);
     const MgLevel& C = H->lv[1];
     if (!encode_map_3d(&H->cmap, C.e, 4, C.D.w, C.D.h, C.D.d, kPCw, kPCh)) H->pair_cap = 0;
+    // TMA-staged fine restriction (PG_MG_RESTRICT_TMA=0 keeps the plain kernel; a diagnostic switch read
+    // per build)
+    const Dims& D0 = H->D0;
+    const char* env = getenv("PG_MG_RESTRICT_TMA");
+    H->restrict_tma = !(env && env[0] == '0') && D0.d % 2 == 0 && D0.h % 2 == 0 && D0.w % 2 == 0 &&
+                      restrict_cap(g) > 0 && encode_map_3d(&H->rgmap, H->flags, 1, D0.w, D0.h, D0.d, kQX, kQY);
     return PG_OK;
 }
 
 // Tensor map of a fine-level float vector with a box of kPEw x by, encoded
 // once per (pointer, box); nullptr when the vector cannot be mapped.
-static const CUtensorMap* vec_map(const MgHierarchy& H, const float* p, int by) {
+static const CUtensorMap* vec_map(const MgHierarchy& H, const float* p, int by, int bx = kPEw) {
     for (auto& m : H.maps)
-        if (m.p == p && m.by == by) return &m.m;
+        if (m.p == p && m.by == by && m.bx == bx) return &m.m;
     MgHierarchy::MapEnt& m = H.maps[H.next_map];
     const Dims& D = H.D0;
-    if (!encode_map_3d(&m.m, p, 4, D.w, D.h, D.d, kPEw, by)) return nullptr;
-    H.next_map = (H.next_map + 1) % 6;
+    if (!encode_map_3d(&m.m, p, 4, D.w, D.h, D.d, bx, by)) return nullptr;
+    H.next_map = (H.next_map + 1) % 8;
     m.p = p;
+    m.bx = bx;
     m.by = by;
     return &m.m;
 }
@@ -1005,6 +1166,30 @@ static void pair(pg_grid* g, const MgHierarchy& H, const PairLaunch& P, int mode
     else if (mode == PR_PROLONG) pair_t<PR_PROLONG, false>(g, H, em, P, a);
     else if (rz) pair_t<PR_PLAIN, true>(g, H, em, P, a);
     else pair_t<PR_PLAIN, false>(g, H, em, P, a);
+}
+
+// The fine restriction of 3D grids with even sides by k_mg_restrict3p;
+// false (nothing launched) when it does not apply.
+static bool restrict_tma(pg_grid* g, const MgHierarchy& H, const float* e, const float* f, float* fc) {
+    if (!H.restrict_tma) return false;
+    const CUtensorMap* em = vec_map(H, e, kQEh, kQEw);
+    const CUtensorMap* fm = em ? vec_map(H, f, kQY, kQX) : nullptr;
+    if (!fm) return false;
+    const Dims& D = H.D0;
+    RestrictArgs a;
+    a.d = (int)D.d;
+    a.h = (int)D.h;
+    a.w = (int)D.w;
+    a.ch = (int)H.lv[1].D.h;
+    a.cw = (int)H.lv[1].D.w;
+    a.dt = (float)H.dt;
+    a.fc = fc;
+    a.tiles_x = (a.w + kQX - 1) / kQX;
+    a.tiles_y = (a.h + kQY - 1) / kQY;
+    const int nb = zwalk_blocks(a.tiles_x * a.tiles_y, a.d / 2, restrict_cap(g));
+    cudaStream_t s = g->stream;
+    PG_LAUNCH(KK_MG_RESTRICT, s, k_mg_restrict3p<<<nb, kQThreads, kQSmem, s>>>(*em, *fm, H.rgmap, a, g->ws.state));
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1138,7 +1323,8 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
         const LV v = view(H, l);
         const MgLevel& C = H.lv[l + 1];
         const i64 nc = C.D.nc();
-        if (l == 0)
+        if (l == 0 && pairs && restrict_tma(g, H, e, f, C.f)) {
+        } else if (l == 0)
             PG_LAUNCH(KK_MG_RESTRICT, s,
                       k_mg_restrict<true><<<blocks_for(g, nc), kMgThreads, 0, s>>>(v, e, f, C.f, (int)C.D.d,
                                                                                  (int)C.D.h, (int)C.D.w,
