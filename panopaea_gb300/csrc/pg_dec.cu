@@ -292,59 +292,62 @@ __device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl)
     return __fadd_rn(s, __fadd_rn(e, __fsub_rn(al, bl)));
 }
 
-// Divisors of the face index split: h w, w, h + 1, w + 1.
-struct FaceDivs {
-    FastDiv hw, w, h1, w1;
-};
-template <class I> inline FaceDivs face_divs(const Dims& D) {
-    return FaceDivs{fast_div_for<I>(D.h * D.w), fast_div_for<I>(D.w), fast_div_for<I>(D.h + 1), fast_div_for<I>(D.w + 1)};
-}
-
+// One thread per index (z, y, x) of the (d+1) x (h+1) x (w+1) box: it
+// computes the x, y and z faces that share that index, so the double-float
+// pressure of a cell is read once for its three low faces (a sweep per face
+// part read it three times); pout (optional) receives p = ph + pl rounded to
+// float, the refined solve's pressure output.
 template <class I>
-__global__ void k_project_df(float* vel, const float* src, const float* __restrict__ ph, const float* __restrict__ pl,
-                             const uint8_t* __restrict__ flags, Dims D, float dt, int zero_solid, FaceDivs fd) {
-    const I nz = (I)D.nfz(), ny = (I)D.nfy(), nf = (I)D.nf();
-    const I h = (I)D.h, w = (I)D.w, hw = h * w, d = (I)D.d;
-    GRID_STRIDE_I(i, nf) {
-        I lo, hi;
-        uint8_t bit;
-        if (i < nz) {
-            I r;
-            const I z = split(i, hw, fd.hw, r);
-            if (z == 0 || z == d) { vel[i] = 0.f; continue; }
-            hi = z * hw + r;
-            lo = hi - hw;
-            bit = ZLO;
-        } else if (i < nz + ny) {
-            const I j = i - nz;
-            I x, y;
-            const I zy = split(j, w, fd.w, x);
-            const I z = split(zy, h + 1, fd.h1, y);
-            if (y == 0 || y == h) { vel[i] = 0.f; continue; }
-            hi = (z * h + y) * w + x;
-            lo = hi - w;
-            bit = YLO;
-        } else {
-            const I j = i - nz - ny;
-            I x;
-            const I zy = split(j, w + 1, fd.w1, x);
-            if (x == 0 || x == w) { vel[i] = 0.f; continue; }
-            hi = zy * w + x;
-            lo = hi - 1;
-            bit = XLO;
-        }
-        const bool open = flags[hi] & bit;
-        const float e = df_diff(ph[lo], pl[lo], ph[hi], pl[hi]);  // p_lo - p_hi = -grad p
+__global__ void k_project_dfj(float* vel, const float* src, const float* __restrict__ ph, const float* __restrict__ pl,
+                              const uint8_t* __restrict__ flags, Dims D, float dt, int zero_solid,
+                              float* __restrict__ pout, FastDiv fexy, FastDiv fex) {
+    const I d = (I)D.d, h = (I)D.h, w = (I)D.w, hw = h * w;
+    const I nz = (I)D.nfz(), ny = (I)D.nfy();
+    const bool three = D.nd == 3;
+    const I ex = w + 1, exy = (h + 1) * ex;
+    const I n = (three ? d + 1 : d) * exy;
+    auto face = [&](I i, I lo, I c, uint8_t bit, float chh, float chl) {
+        const bool open = flags[c] & bit;
+        const float e = df_diff(ph[lo], pl[lo], chh, chl);  // p_lo - p_hi = -grad p
         vel[i] = (zero_solid && !open) ? 0.f : __fadd_rn(src[i], __fmul_rn(dt, e));
+    };
+    GRID_STRIDE_I(t, n) {
+        I r, x;
+        const I z = split(t, exy, fexy, r);
+        const I y = split(r, ex, fex, x);
+        const I c = (z * h + y) * w + x;
+        float chh = 0.f, chl = 0.f;
+        if (z < d && y < h && x < w) {
+            chh = ph[c];
+            chl = pl[c];
+            if (pout) pout[c] = __fadd_rn(chh, chl);
+        }
+        if (z < d && y < h) {  // x face (z, y, x)
+            const I i = nz + ny + (z * h + y) * (w + 1) + x;
+            if (x == 0 || x == w) vel[i] = 0.f;
+            else face(i, c - 1, c, XLO, chh, chl);
+        }
+        if (z < d && x < w) {  // y face (z, y, x)
+            const I i = nz + (z * (h + 1) + y) * w + x;
+            if (y == 0 || y == h) vel[i] = 0.f;
+            else face(i, c - w, c, YLO, chh, chl);
+        }
+        if (three && y < h && x < w) {  // z face (z, y, x)
+            const I i = c;
+            if (z == 0 || z == d) vel[i] = 0.f;
+            else face(i, c - hw, c, ZLO, chh, chl);
+        }
     }
 }
 
 int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid,
-                      const float* src) {
+                      const float* src, float* pout) {
     const Dims& D = g->dims;
+    const i64 n = (D.nd == 3 ? D.d + 1 : D.d) * (D.h + 1) * (D.w + 1);
     PG_IDX(g, PG_LAUNCH(KK_PROJECT, g->stream,
-              k_project_df<I><<<grid_blocks(g, D.nf(), kThreads), kThreads, 0, g->stream>>>(
-                  vel, src ? src : vel, ph, pl, g->flags, D, (float)dt, zero_solid, face_divs<I>(D))));
+              k_project_dfj<I><<<grid_blocks(g, n, kThreads), kThreads, 0, g->stream>>>(
+                  vel, src ? src : vel, ph, pl, g->flags, D, (float)dt, zero_solid, pout,
+                  fast_div_for<I>((D.h + 1) * (D.w + 1)), fast_div_for<I>(D.w + 1))));
     PG_CHECK_LAUNCH();
     return PG_OK;
 }

@@ -16,7 +16,7 @@ template <class T>
 int launch_project(const pg_grid* g, T* vel, const T* p, double dt, int zero_solid, const T* src);
 int launch_project_p64(const pg_grid* g, float* vel, const double* p, double dt, int zero_solid, const float* src);
 int launch_project_df(const pg_grid* g, float* vel, const float* ph, const float* pl, double dt, int zero_solid,
-                      const float* src);
+                      const float* src, float* pout);
 template <class T> int launch_walls(const pg_grid* g, T* vel);
 template <class T> int launch_source_box(const pg_grid* g, T* rho, T* vel, const pg_step_params* prm);
 template <class T> int launch_source_field(const pg_grid* g, T* rho, const T* src);
@@ -424,8 +424,11 @@ static int solve_plain(pg_grid* g, const pg_solver_params* prm, T* x, const T* b
 }
 
 // FP32 CG rounds inside FP64 residual refinement.
+// store_x = false leaves x to the caller (the step's projection writes it
+// from the double-float x it reads anyway); the FP64-class x stays in the
+// grid's kX64 buffer either way.
 static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, const float* b, double dt,
-                         pg_pcg_stats* st, ZHook* hook = nullptr) {
+                         pg_pcg_stats* st, ZHook* hook = nullptr, bool store_x = true) {
     Extras* ex = extras_of(g);
     const i64 n = g->dims.nc();
     int rc;
@@ -551,7 +554,7 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
     if (!x_set) PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
     if (native)
         PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_store<<<nb, kThreads, 0, g->stream>>>(x, (const double*)x64, n));
-    else
+    else if (store_x)
         PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_xdf_store<<<nb, kThreads, 0, g->stream>>>(x, xh, xl, n));
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(g->stream));
@@ -642,7 +645,17 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, R* rho, T* pressure, pg_
     if ((rc = launch_rhs<T>(g, (T*)b, av))) return rc;
     // pressure solve (dec_fluid.rs:87-121)
     pg_pcg_stats s{};
-    if ((rc = solve_pressure<T>(g, &prm->solver, pressure, (const T*)b, dt, &s))) return rc;
+    // double-float refinement: the projection below also stores the pressure
+    const bool df = sizeof(T) == 4 && prm->solver.refine > 0 && !prm->solver.fp64_native;
+    if (df) {
+        const pg_solver_params* sp = &prm->solver;
+        if (sp->precond < PG_PRECOND_NONE || sp->precond > PG_PRECOND_MG) return bad_arg("solver: unknown precond");
+        if (sp->max_iter < 0) return bad_arg("solver: max_iter < 0");
+        rc = solve_refined(g, sp, (float*)pressure, (const float*)b, dt, &s, nullptr, false);
+    } else {
+        rc = solve_pressure<T>(g, &prm->solver, pressure, (const T*)b, dt, &s);
+    }
+    if (rc) return rc;
     // projection + walls (dec_fluid.rs:123-141); after a refined solve the
     // gradient is taken from the FP64 pressure it accumulated.
     if (sizeof(T) == 4 && prm->solver.refine > 0) {
@@ -653,7 +666,7 @@ int step(pg_grid* g, const pg_step_params* prm, T* vel, R* rho, T* pressure, pg_
                                     (const float*)av);
         else
             rc = launch_project_df(g, (float*)vel, (const float*)x64, (const float*)x64 + nc, dt,
-                                   prm->zero_solid_after_project, (const float*)av);
+                                   prm->zero_solid_after_project, (const float*)av, (float*)pressure);
         if (rc) return rc;
     } else if ((rc = launch_project<T>(g, vel, pressure, dt, prm->zero_solid_after_project, av))) {
         return rc;
