@@ -257,6 +257,12 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
 }
+// Zero 8 consecutive 32-bit columns of this thread's lane.
+__device__ __forceinline__ void st8_zero(uint32_t taddr) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(0u)
+                 : "memory");
+}
+
 // 8 consecutive 32-bit columns of this thread's lane.
 __device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
     uint32_t r[8];
@@ -269,18 +275,33 @@ __device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Small output channel counts merge the three z taps into one MMA: an input
+// brick plane bs feeds output planes bs, bs - 1 and bs - 2 through the taps
+// dz = 0, 1, 2 with the same A operand, so their weights are stacked along N
+// (N' = 3 N) and the planes' accumulators are laid out in reverse order
+// (plane t at column (TZ + 1 - t) N): one MMA per input plane and (dx, dy)
+// writes the three planes' columns.  Planes -2, -1, TZ, TZ + 1 take the edge
+// products that no output needs.  Half the A-operand reads of the 27-tap
+// loop, for the layers whose MMA is bound by that shared-memory traffic.
+__host__ __device__ constexpr bool merge_dz(int n) { return n <= 32; }
+
 template <int COUT> struct Cfg {
+    static constexpr bool kMerge = merge_dz(COUT);
     static constexpr int TZ = COUT >= 96 ? 2 : 4;
     static constexpr int BZ = TZ + 2;
     static constexpr int kPlane = BX * BY * BZ * 16;      // one 8-channel half of the brick
     static constexpr int kBrick = 2 * kPlane;             // one 16-channel chunk
     static constexpr int kWTap = 2 * COUT * 16;           // one tap of one chunk
+    static constexpr int kWTap9 = 3 * kWTap;              // merged: the three z taps of one (dx, dy)
     static constexpr int kWChunk = 27 * kWTap;
     static constexpr int kBrickOff = 128, kWOff = kBrickOff + kBrick;
     static constexpr size_t kSmem = 128 + (size_t)kBrick + kWChunk;
-    static constexpr int kCols = TZ * COUT <= 32 ? 32 : (TZ * COUT <= 64 ? 64 : (TZ * COUT <= 128 ? 128 : (TZ * COUT <= 256 ? 256 : 512)));
-    static_assert(TZ * COUT <= 512, "accumulators must fit in tensor memory");
+    static constexpr int kAccCols = kMerge ? (TZ + 4) * COUT : TZ * COUT;
+    static constexpr int kCols = kAccCols <= 32 ? 32 : (kAccCols <= 64 ? 64 : (kAccCols <= 128 ? 128 : (kAccCols <= 256 ? 256 : 512)));
+    static_assert(kAccCols <= 512, "accumulators must fit in tensor memory");
     static_assert(kPlane % 16 == 0 && kBrick % 128 == 0, "operand alignment");
+    // tensor-memory column of output plane t's accumulator
+    __host__ __device__ static constexpr int col(int t) { return kMerge ? (TZ + 1 - t) * COUT : t * COUT; }
 };
 
 struct Geom {
@@ -318,6 +339,15 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const bf16* __restrict__ i
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
+    if (C::kMerge) {  // every merged MMA accumulates: start the accumulators at zero
+        if (warp < 4) {
+            for (int c = 0; c < C::kAccCols; c += 8) st8_zero(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c);
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+    }
     bool ok = true;  // block-uniform
     int committed = -1;
     for (int kc = 0; kc < KC; ++kc) {
@@ -350,15 +380,29 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const bf16* __restrict__ i
         if (tid == 0) {
             fence_after();
             const uint32_t bs = smem_u32(brick), ws = smem_u32(wsm);
+            if (C::kMerge) {
+                constexpr uint32_t kIdesc3 = idesc_bf16(128, 3 * COUT);
 #pragma unroll 1
-            for (int tap = 0; tap < 27; ++tap) {
-                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-                const uint64_t bdesc = sdesc(ws + tap * C::kWTap, COUT * 16, 128);
+                for (int tap9 = 0; tap9 < 9; ++tap9) {
+                    const int dy = tap9 / 3, dx = tap9 % 3;
+                    const uint64_t bdesc = sdesc(ws + tap9 * C::kWTap9, 3 * COUT * 16, 128);
 #pragma unroll
-                for (int tz = 0; tz < TZ; ++tz) {
-                    const uint32_t a = bs + (uint32_t)((((tz + dz) * BY + dy) * BX + dx) * 16);
-                    mma(tmem + (uint32_t)(tz * COUT), sdesc(a, C::kPlane, BX * 16), bdesc, kIdesc,
-                        (kc > 0 || tap > 0) ? 1u : 0u);
+                    for (int pz = 0; pz < C::BZ; ++pz) {
+                        const uint32_t a = bs + (uint32_t)(((pz * BY + dy) * BX + dx) * 16);
+                        mma(tmem + (uint32_t)C::col(pz), sdesc(a, C::kPlane, BX * 16), bdesc, kIdesc3, 1u);
+                    }
+                }
+            } else {
+#pragma unroll 1
+                for (int tap = 0; tap < 27; ++tap) {
+                    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                    const uint64_t bdesc = sdesc(ws + tap * C::kWTap, COUT * 16, 128);
+#pragma unroll
+                    for (int tz = 0; tz < TZ; ++tz) {
+                        const uint32_t a = bs + (uint32_t)((((tz + dz) * BY + dy) * BX + dx) * 16);
+                        mma(tmem + (uint32_t)(tz * COUT), sdesc(a, C::kPlane, BX * 16), bdesc, kIdesc,
+                            (kc > 0 || tap > 0) ? 1u : 0u);
+                    }
                 }
             }
             commit(bar);
@@ -394,7 +438,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const bf16* __restrict__ i
 #pragma unroll 1
             for (int cg = 0; cg < COUT / 8; ++cg) {
                 float v[8];
-                ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(tz * COUT + cg * 8), v);
+                ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(C::col(tz) + cg * 8), v);
                 if (!in_grid) continue;
                 if (epi == EPI_RELU) {
 #pragma unroll
@@ -428,17 +472,33 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const bf16* __restrict__ i
 // K index k = 16 chunk + 8 half + j an input channel of the convolution and
 // n an output channel; forward W[tap][k][n], backward-data (transposed,
 // tap-mirrored) W[26 - tap][n][k] of the forward layer.
+// With merge_dz(N) the three z taps of one (dx, dy) are stacked along N:
+// wtc[chunk][dy 3 + dx][half][dz N + n][8].
 __global__ void k_wprep_tc(const float* __restrict__ W, int cin, int cout, int transposed, bf16* __restrict__ wtc) {
     const int K = transposed ? cout : cin, N = transposed ? cin : cout;
+    const bool merged = merge_dz(N);
     const int n_all = 27 * K * N;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_all; i += gridDim.x * blockDim.x) {
         const int j = i & 7;
         int r = i >> 3;
-        const int n = r % N;
-        r /= N;
-        const int hf = r & 1;
-        r >>= 1;
-        const int tap = r % 27, kc = r / 27;
+        int n, hf, tap, kc;
+        if (merged) {
+            const int nn = r % (3 * N);
+            r /= 3 * N;
+            hf = r & 1;
+            r >>= 1;
+            const int tap9 = r % 9;
+            kc = r / 9;
+            n = nn % N;
+            tap = (nn / N) * 9 + tap9;
+        } else {
+            n = r % N;
+            r /= N;
+            hf = r & 1;
+            r >>= 1;
+            tap = r % 27;
+            kc = r / 27;
+        }
         const int k = kc * 16 + hf * 8 + j;
         const float v = transposed ? W[((size_t)(26 - tap) * cin + n) * cout + k] : W[((size_t)tap * cin + k) * cout + n];
         wtc[i] = __float2bfloat16_rn(v);
