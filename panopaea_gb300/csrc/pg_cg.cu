@@ -118,14 +118,18 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(T* __restrict__ x, T* __
 // the only reduction is the order-independent ||b||inf); n4 = n / 4.
 __global__ void __launch_bounds__(kCgThreads)
     k_cg_init4(float4* __restrict__ x, float4* __restrict__ r, const float4* __restrict__ b, i64 n4, double thr,
-               double rel_tol, i64 max_iter, int zero_x, CgState* st, double* partials, double nfluid) {
+               double rel_tol, i64 max_iter, int zero_x, CgState* st, double* partials, double nfluid,
+               float4* __restrict__ xl) {
     __shared__ double sm[32];
     float bm = 0.f;
     int bad = 0;
     float sb = 0.f;  // sum(b) for the lazy projection (feeds a small correction term)
     for (i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x; c < n4; c += (i64)gridDim.x * blockDim.x) {
         const float4 bv = b[c];
-        if (zero_x) x[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (zero_x) {
+            x[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (xl) xl[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         r[c] = bv;
         bm = fmaxf(fmaxf(fmaxf(bm, fabsf(bv.x)), fmaxf(fabsf(bv.y), fabsf(bv.z))), fabsf(bv.w));
         bad |= !isfinite(bv.x) | !isfinite(bv.y) | !isfinite(bv.z) | !isfinite(bv.w);
@@ -380,13 +384,30 @@ __global__ void __launch_bounds__(kCgThreads)
     }
 }
 
+// x + alpha p into the double-float pair (xh, xl): the product's rounding
+// error (fma) and the sum's (TwoSum) both go into the low part, so the
+// iterate carries the sum of its increments to ~48 bits.
+__device__ __forceinline__ void df_axpy(float& xh, float& xl, float alpha, float p) {
+    const float d = __fmul_rn(alpha, p);
+    const float de = __fmaf_rn(alpha, p, -d);
+    const float s = __fadd_rn(xh, d);
+    const float bb = __fsub_rn(s, xh);
+    const float e = __fadd_rn(__fsub_rn(xh, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+    const float lo = __fadd_rn(xl, __fadd_rn(e, de));
+    const float h2 = __fadd_rn(s, lo);
+    xh = h2;
+    xl = __fsub_rn(lo, __fsub_rn(h2, s));
+}
+
 // The update of the MG path (z.r comes from the V-cycle, so the only
 // reduction is the order-independent ||r||inf) on float4 vectors, two per
 // thread and iteration: eight cells' x, p, r, Ap in flight per thread.  Same
-// per-cell arithmetic as k_cg_update<float, PM_ZBUF>; n4 = n / 4.
+// per-cell arithmetic as k_cg_update<float, PM_ZBUF>; n4 = n / 4.  With DFX
+// the iterate is the double-float pair (x, xl), updated by df_axpy.
+template <bool DFX>
 __global__ void __launch_bounds__(kCgThreads)
     k_cg_update4(float4* __restrict__ x, float4* __restrict__ r, const float4* p0, const float4* p1,
-                 const float4* __restrict__ ap, i64 n4, CgState* st, double* partials) {
+                 const float4* __restrict__ ap, i64 n4, CgState* st, double* partials, float4* __restrict__ xl) {
     if (st->done) return;
     __shared__ double sm[32];
     const i64 k = *(volatile const i64*)&st->iter;
@@ -397,10 +418,20 @@ __global__ void __launch_bounds__(kCgThreads)
     auto one = [&](i64 c) {
         const float4 xv = x[c], pv = p[c], rv = r[c], av = ap[c];
         float4 xo, ro;
-        xo.x = xv.x + alpha * pv.x;
-        xo.y = xv.y + alpha * pv.y;
-        xo.z = xv.z + alpha * pv.z;
-        xo.w = xv.w + alpha * pv.w;
+        if (DFX) {
+            float4 lo = xl[c];
+            xo = xv;
+            df_axpy(xo.x, lo.x, alpha, pv.x);
+            df_axpy(xo.y, lo.y, alpha, pv.y);
+            df_axpy(xo.z, lo.z, alpha, pv.z);
+            df_axpy(xo.w, lo.w, alpha, pv.w);
+            xl[c] = lo;
+        } else {
+            xo.x = xv.x + alpha * pv.x;
+            xo.y = xv.y + alpha * pv.y;
+            xo.z = xv.z + alpha * pv.z;
+            xo.w = xv.w + alpha * pv.w;
+        }
         ro.x = rv.x + nalpha * av.x;
         ro.y = rv.y + nalpha * av.y;
         ro.z = rv.z + nalpha * av.z;
@@ -536,6 +567,18 @@ __global__ void __launch_bounds__(kCgThreads)
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
+template <class T>
+static bool cg_dfx_ok(const CgBuffers<T>& buf, i64 n, const uint8_t* flags) {
+    return sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.xl) && aligned16(buf.r) &&
+           aligned16(buf.b) && aligned16(buf.p[0]) && aligned16(buf.p[1]) && aligned16(buf.ap) && aligned16(flags);
+}
+
+bool cg_dfx_supported(const pg_grid* g, const CgBuffers<float>& buf) {
+    const char* env = getenv("PG_CG_DFX");
+    if (env && env[0] == '0') return false;
+    return cg_dfx_ok(buf, g->dims.nc(), g->flags);
+}
+
 // After max_iterations the reference has already run aux = M r and
 // search = aux + beta*search (pcg.rs:65-77); reproduce that tail.
 template <class T, int PM>
@@ -568,11 +611,17 @@ static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook
     const i64 n = D.nc();
     const bool vec4 = sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.r) &&
                       aligned16(buf.p[0]) && aligned16(buf.p[1]) && aligned16(buf.ap) && aligned16(g->flags);
-    if (PM == PM_ZBUF && vec4)
+    if (PM == PM_ZBUF && vec4 && buf.xl)
         PG_LAUNCH(KK_CG_UPDATE, s,
-                  k_cg_update4<<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.p[0],
-                                                         (const float4*)buf.p[1], (const float4*)buf.ap, n / 4,
-                                                         g->ws.state, g->ws.partials));
+                  k_cg_update4<true><<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.p[0],
+                                                               (const float4*)buf.p[1], (const float4*)buf.ap, n / 4,
+                                                               g->ws.state, g->ws.partials, (float4*)buf.xl));
+    else if (PM == PM_ZBUF && vec4)
+        PG_LAUNCH(KK_CG_UPDATE, s,
+                  k_cg_update4<false><<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r,
+                                                                (const float4*)buf.p[0], (const float4*)buf.p[1],
+                                                                (const float4*)buf.ap, n / 4, g->ws.state,
+                                                                g->ws.partials, nullptr));
     else if (PM != PM_ZBUF && vec4)
         PG_LAUNCH(KK_CG_UPDATE, s,
                   k_cg_update4r<PM><<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r,
@@ -598,7 +647,7 @@ __global__ void k_cg_cond(const CgState* st, cudaGraphConditionalHandle h) {
 struct CgGraph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    const void* key[8] = {};
+    const void* key[9] = {};
     double dt = 0.0;
     int pm = -1, nd = 0;
     uintptr_t hook_key = 0;
@@ -626,11 +675,11 @@ template <class T, int PM>
 static int get_graph(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* hook, CgGraph** out) {
     if (!g->ws.graphs) g->ws.graphs = new CgGraphCache();
     CgGraphCache* C = (CgGraphCache*)g->ws.graphs;
-    const void* key[8] = {buf.x, buf.b, buf.r, buf.ap, buf.p[0], buf.p[1], buf.z, g->flags};
+    const void* key[9] = {buf.x, buf.b, buf.r, buf.ap, buf.p[0], buf.p[1], buf.z, g->flags, buf.xl};
     const uintptr_t hk = hook ? hook->key() : 0;
     for (auto& e : C->e) {
         if (e.exec && e.pm == PM && e.dt == (double)dt && e.nd == g->dims.nd && e.hook_key == hk &&
-            std::equal(key, key + 8, e.key)) {
+            std::equal(key, key + 9, e.key)) {
             *out = &e;
             return PG_OK;
         }
@@ -672,7 +721,7 @@ static int get_graph(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* h
         return cuda_fail(err, "CG graph capture");
     }
     PG_CUDA(cudaGraphInstantiate(&E.exec, E.graph, 0));
-    std::copy(key, key + 8, E.key);
+    std::copy(key, key + 9, E.key);
     E.pm = PM;
     E.dt = (double)dt;
     E.nd = g->dims.nd;
@@ -691,12 +740,15 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
     const int nb = grid_blocks(g, n, kCgThreads, 8);
     Workspace& ws = g->ws;
     cudaStream_t s = g->stream;
+    // The double-float iterate exists only in the float4 kernels.
+    if (buf.xl && (PM != PM_ZBUF || !cg_dfx_ok(buf, n, g->flags)))
+        return bad_arg("run_cg: a double-float iterate needs the float4 MG path");
     PG_CUDA(cudaMemsetAsync(ws.state, 0, sizeof(CgState), s));
     if (PM == PM_ZBUF && sizeof(T) == 4 && n % 4 == 0 && aligned16(buf.x) && aligned16(buf.r) && aligned16(buf.b))
         PG_LAUNCH(KK_CG_INIT, s,
                   k_cg_init4<<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r, (const float4*)buf.b, n / 4,
                                                        cfg.threshold, cfg.rel_tol, cfg.max_iter, cfg.zero_x,
-                                                       ws.state, ws.partials, cfg.nfluid));
+                                                       ws.state, ws.partials, cfg.nfluid, (float4*)buf.xl));
     else
         PG_LAUNCH(KK_CG_INIT, s,
               k_cg_init<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.b, g->flags, n, dt, cfg.threshold,

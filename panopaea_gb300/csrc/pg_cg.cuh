@@ -16,7 +16,8 @@ template <class T> struct CgBuffers {
     T* r;
     T* ap;
     T* p[2];
-    T* z = nullptr;  // PM_ZBUF only
+    T* z = nullptr;   // PM_ZBUF only
+    T* xl = nullptr;  // PM_ZBUF, float, n % 4 == 0: x held as the double-float pair (x, xl)
 };
 
 struct CgConfig {
@@ -82,6 +83,11 @@ struct ZHook {
 // pg_status for launch/CUDA failures; the solve outcome is in *stats.
 template <class T>
 int run_cg(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_stats* stats, ZHook* hook = nullptr);
+
+// Whether run_cg with MG preconditioning can carry x as the double-float pair
+// (buf.x, buf.xl): float4-aligned buffers and flags, cells a multiple of 4.
+// PG_CG_DFX=0 turns it off (a diagnostic switch).
+bool cg_dfx_supported(const pg_grid* g, const CgBuffers<float>& buf);
 
 // Device side: fold a freshly reduced z.r into the CG state.  Right after
 // init (iter == 0) it is sigma; afterwards beta = z.r / sigma (pcg.rs:67-68).

@@ -489,6 +489,22 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
         const bool from_b = rounds == 0 && !guess;
         CgBuffers<float> buf{(float*)d, from_b ? b : (const float*)rin, (float*)rr, (float*)ap,
                              {(float*)p0, (float*)p1}};
+        // Round 0 of the MG path accumulates x = 0 + sum(alpha p) straight
+        // into the double-float iterate (no k_xdf_set).  An FP32 iterate
+        // floors the true residual near 2e-6 of ||b|| (the FP32 sum of a few
+        // long steps), so FP32 rounds are asked for no more than 1e-5 and a
+        // second round follows; the double-float one is asked for the
+        // target itself and usually ends the solve.
+        bool dfx = false;
+        if (from_b && !native && !hook && prm->precond == PG_PRECOND_MG) {
+            CgBuffers<float> b2 = buf;
+            b2.x = xh;
+            b2.xl = xl;
+            if (cg_dfx_supported(g, b2)) {
+                buf = b2;
+                dfx = true;
+            }
+        }
         CgConfig cfg{prm->precond, prm->max_iter, 0.0, 0.0, dt, prm->check_every, 1};
         if (from_b && !prm->rel_stop) {
             cfg.threshold = 0.5 * prm->threshold;
@@ -500,7 +516,7 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
                 cfg.rel_tol = std::min(prm->inner_rel_tol, 0.5);
             } else {
                 const double inner = from_b ? 0.5 * prm->rel_tol : 0.5 * target / rmax;
-                cfg.rel_tol = std::min(std::max(inner, 1e-5), 0.5);
+                cfg.rel_tol = std::min(std::max(inner, dfx ? 0.0 : 1e-5), 0.5);
             }
         }
         pg_pcg_stats s{};
@@ -526,7 +542,9 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
             out.status = s.status;
             break;
         }
-        if (from_b) {  // x was 0: x = d
+        if (dfx) {
+            // x already holds the round's iterate
+        } else if (from_b) {  // x was 0: x = d
             if (native)
                 PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_set<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
             else
