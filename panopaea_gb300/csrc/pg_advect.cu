@@ -75,71 +75,106 @@ __global__ void k_advect_mac_2d(T* __restrict__ dst, const T* __restrict__ src, 
     }
 }
 
-// Trilinear face sample of a part with dims (nz, ny, nx).
-template <class T, class I>
-__device__ __forceinline__ T sample_part(const T* __restrict__ q, I nz, I ny, I nx, T ppx, T ox, T ppy, T oy,
-                                         T ppz, T oz) {
+// The three face parts of a 3D MAC field: part 0 = z faces (d+1, h, w) at
+// offset 0, part 1 = y faces (d, h+1, w), part 2 = x faces (d, h, w+1).
+// Every 3D MAC advection sample reads its velocity and source values
+// through an accessor, so the plain and the shared-memory-staged kernels run
+// the same arithmetic on the same values.
+template <class T, class I> struct MacGlobal {
+    const T* vel;
+    const T* src;
+    I d, h, w;
+    __device__ __forceinline__ I nz() const { return (d + 1) * h * w; }
+    __device__ __forceinline__ I ny() const { return d * (h + 1) * w; }
+    __device__ __forceinline__ I ix(I z, I y, I x) const { return nz() + ny() + (z * h + y) * (w + 1) + x; }
+    __device__ __forceinline__ I iy(I z, I y, I x) const { return nz() + (z * (h + 1) + y) * w + x; }
+    __device__ __forceinline__ I iz(I z, I y, I x) const { return (z * h + y) * w + x; }
+    __device__ __forceinline__ T vx(I z, I y, I x) const { return vel[ix(z, y, x)]; }
+    __device__ __forceinline__ T vy(I z, I y, I x) const { return vel[iy(z, y, x)]; }
+    __device__ __forceinline__ T vz(I z, I y, I x) const { return vel[iz(z, y, x)]; }
+    // The 8 source values around a sample of part p: c[4 * zi + 2 * yi + xi].
+    __device__ __forceinline__ void gather(int p, I z0, I z1, I y0, I y1, I x0, I x1, T c[8]) const {
+        const I nyp = p == 1 ? h + 1 : h, nxp = p == 2 ? w + 1 : w;
+        const T* q = src + (p == 0 ? I(0) : p == 1 ? nz() : nz() + ny());
+        const T* a0 = q + z0 * nyp * nxp;
+        const T* a1 = q + z1 * nyp * nxp;
+        c[0] = a0[y0 * nxp + x0];
+        c[1] = a0[y0 * nxp + x1];
+        c[2] = a0[y1 * nxp + x0];
+        c[3] = a0[y1 * nxp + x1];
+        c[4] = a1[y0 * nxp + x0];
+        c[5] = a1[y0 * nxp + x1];
+        c[6] = a1[y1 * nxp + x0];
+        c[7] = a1[y1 * nxp + x1];
+    }
+};
+
+// Trilinear face sample of part p with dims (nz, ny, nx).
+template <class T, class I, class A>
+__device__ __forceinline__ T sample_part(const A& acc, int p, I nz, I ny, I nx, T ppx, T ox, T ppy, T oy, T ppz,
+                                         T oz) {
     I x0, x1, y0, y1, z0, z1;
     T s, t, u;
     face_coord(ppx, ox, nx, x0, x1, s);
     face_coord(ppy, oy, ny, y0, y1, t);
     face_coord(ppz, oz, nz, z0, z1, u);
-    const T* a0 = q + z0 * ny * nx;
-    const T* a1 = q + z1 * ny * nx;
-    const T b0 = bilerp(a0[y0 * nx + x0], a0[y0 * nx + x1], a0[y1 * nx + x0], a0[y1 * nx + x1], s, t);
-    const T b1 = bilerp(a1[y0 * nx + x0], a1[y0 * nx + x1], a1[y1 * nx + x0], a1[y1 * nx + x1], s, t);
+    T c[8];
+    acc.gather(p, z0, z1, y0, y1, x0, x1, c);
+    const T b0 = bilerp(c[0], c[1], c[2], c[3], s, t);
+    const T b1 = bilerp(c[4], c[5], c[6], c[7], s, t);
     return lerp_ref(b0, b1, u);
+}
+
+// The x, y and z faces that share index (z, y, x) of the (d+1) x (h+1) x
+// (w+1) box (those that exist), advected into dst.
+template <class T, class I, class A>
+__device__ __forceinline__ void mac3_index(const A& acc, const MacGlobal<T, I>& G, T* __restrict__ dst, T ndt, I z,
+                                           I y, I x) {
+    const I d = G.d, h = G.h, w = G.w;
+    if (z < d && y < h) {  // x face (z, y, x), part dims (d, h, w+1)
+        const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
+        const T vx_ = acc.vx(z, y, x);
+        const T vy_ = avg4(acc.vy(z, y, xc), acc.vy(z, y + 1, xc), acc.vy(z, y, xm), acc.vy(z, y + 1, xm));
+        const T vz_ = avg4(acc.vz(z, y, xc), acc.vz(z + 1, y, xc), acc.vz(z, y, xm), acc.vz(z + 1, y, xm));
+        dst[G.ix(z, y, x)] = sample_part<T, I>(acc, 2, d, h, w + 1, back(add_rn((T)x, T(0)), ndt, vx_), T(0),
+                                               back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5),
+                                               back(add_rn((T)z, T(0.5)), ndt, vz_), T(0.5));
+    }
+    if (z < d && x < w) {  // y face (z, y, x), part dims (d, h+1, w)
+        const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
+        const T vx_ = avg4(acc.vx(z, yc, x), acc.vx(z, yc, x + 1), acc.vx(z, ym, x), acc.vx(z, ym, x + 1));
+        const T vy_ = acc.vy(z, y, x);
+        const T vz_ = avg4(acc.vz(z, yc, x), acc.vz(z + 1, yc, x), acc.vz(z, ym, x), acc.vz(z + 1, ym, x));
+        dst[G.iy(z, y, x)] = sample_part<T, I>(acc, 1, d, h + 1, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
+                                               back(add_rn((T)y, T(0)), ndt, vy_), T(0),
+                                               back(add_rn((T)z, T(0.5)), ndt, vz_), T(0.5));
+    }
+    if (y < h && x < w) {  // z face (z, y, x), part dims (d+1, h, w)
+        const I zc = z < d - 1 ? z : d - 1, zm = z > 0 ? z - 1 : 0;
+        const T vx_ = avg4(acc.vx(zc, y, x), acc.vx(zc, y, x + 1), acc.vx(zm, y, x), acc.vx(zm, y, x + 1));
+        const T vy_ = avg4(acc.vy(zc, y, x), acc.vy(zc, y + 1, x), acc.vy(zm, y, x), acc.vy(zm, y + 1, x));
+        const T vz_ = acc.vz(z, y, x);
+        dst[G.iz(z, y, x)] = sample_part<T, I>(acc, 0, d + 1, h, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
+                                               back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5),
+                                               back(add_rn((T)z, T(0)), ndt, vz_), T(0));
+    }
 }
 
 // advect_mac, 3D extension
 template <class T, class I>
 __global__ void k_advect_mac_3d(T* __restrict__ dst, const T* __restrict__ src, const T* __restrict__ vel, Dims D,
                                 T ndt, FastDiv fexy, FastDiv fex) {
-    const I d = (I)D.d, h = (I)D.h, w = (I)D.w;
-    const I nz = (I)D.nfz(), ny = (I)D.nfy();
-    auto FX = [&](I z, I y, I x) { return nz + ny + (z * h + y) * (w + 1) + x; };
-    auto FY = [&](I z, I y, I x) { return nz + (z * (h + 1) + y) * w + x; };
-    auto FZ = [&](I z, I y, I x) { return (z * h + y) * w + x; };
-    const T* qz = src;
-    const T* qy = src + nz;
-    const T* qx = src + nz + ny;
+    const MacGlobal<T, I> G{vel, src, (I)D.d, (I)D.h, (I)D.w};
     // One thread per index (z, y, x) of the (d+1) x (h+1) x (w+1) box: it
     // computes the x, y and z faces that share that index, so the gathers of
     // the three components hit the same cache lines (processing the three
     // parts one after another re-reads each part from DRAM).
-    const I ex = w + 1, exy = (h + 1) * ex;
-    GRID_STRIDE(t, (d + 1) * exy) {
+    const I ex = G.w + 1, exy = (G.h + 1) * ex;
+    GRID_STRIDE(t, (G.d + 1) * exy) {
         I r, x;
         const I z = split(t, exy, fexy, r);
         const I y = split(r, ex, fex, x);
-        if (z < d && y < h) {  // x face (z, y, x), part dims (d, h, w+1)
-            const I i = FX(z, y, x);
-            const I xc = x < w - 1 ? x : w - 1, xm = x > 0 ? x - 1 : 0;
-            const T vx_ = vel[i];
-            const T vy_ = avg4(vel[FY(z, y, xc)], vel[FY(z, y + 1, xc)], vel[FY(z, y, xm)], vel[FY(z, y + 1, xm)]);
-            const T vz_ = avg4(vel[FZ(z, y, xc)], vel[FZ(z + 1, y, xc)], vel[FZ(z, y, xm)], vel[FZ(z + 1, y, xm)]);
-            dst[i] = sample_part(qx, d, h, w + 1, back(add_rn((T)x, T(0)), ndt, vx_), T(0),
-                                 back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0.5)), ndt, vz_),
-                                 T(0.5));
-        }
-        if (z < d && x < w) {  // y face (z, y, x), part dims (d, h+1, w)
-            const I i = FY(z, y, x);
-            const I yc = y < h - 1 ? y : h - 1, ym = y > 0 ? y - 1 : 0;
-            const T vx_ = avg4(vel[FX(z, yc, x)], vel[FX(z, yc, x + 1)], vel[FX(z, ym, x)], vel[FX(z, ym, x + 1)]);
-            const T vy_ = vel[i];
-            const T vz_ = avg4(vel[FZ(z, yc, x)], vel[FZ(z + 1, yc, x)], vel[FZ(z, ym, x)], vel[FZ(z + 1, ym, x)]);
-            dst[i] = sample_part(qy, d, h + 1, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
-                                 back(add_rn((T)y, T(0)), ndt, vy_), T(0), back(add_rn((T)z, T(0.5)), ndt, vz_), T(0.5));
-        }
-        if (y < h && x < w) {  // z face (z, y, x), part dims (d+1, h, w)
-            const I i = FZ(z, y, x);
-            const I zc = z < d - 1 ? z : d - 1, zm = z > 0 ? z - 1 : 0;
-            const T vx_ = avg4(vel[FX(zc, y, x)], vel[FX(zc, y, x + 1)], vel[FX(zm, y, x)], vel[FX(zm, y, x + 1)]);
-            const T vy_ = avg4(vel[FY(zc, y, x)], vel[FY(zc, y + 1, x)], vel[FY(zm, y, x)], vel[FY(zm, y + 1, x)]);
-            const T vz_ = vel[i];
-            dst[i] = sample_part(qz, d + 1, h, w, back(add_rn((T)x, T(0.5)), ndt, vx_), T(0.5),
-                                 back(add_rn((T)y, T(0.5)), ndt, vy_), T(0.5), back(add_rn((T)z, T(0)), ndt, vz_), T(0));
-        }
+        mac3_index(G, G, dst, ndt, z, y, x);
     }
 }
 

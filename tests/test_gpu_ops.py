@@ -166,6 +166,25 @@ def test_advection(pg, oracle, dims, dtype, speed):
     same(host(outf), oracle.advect_mac(vel, dt, vel, dims))
 
 
+@pytest.mark.parametrize("dims", [(70, 50, 90), (33, 17, 65), (9, 40, 100)])
+def test_self_advection_3d_mixed_speeds(pg, oracle, dims):
+    """3D self-advection of a smooth field with sparse fast faces and NaN
+    velocities, at sizes with many blocks: bit-exact against the oracle."""
+    r = rng(seed_of(("staged", dims)))
+    g = make_grid(pg, dims)
+    nf = oracle.num_faces(dims)
+    # smooth part (|v| dt up to ~2.5 cells) plus sparse fast faces and NaNs
+    t = np.arange(nf, dtype=np.float64)
+    vel = (2.5 * np.sin(t * 0.0007) + 0.2 * r.standard_normal(nf)).astype(np.float32)
+    vel[r.integers(0, nf, nf // 50)] = 9.0
+    vel[r.integers(0, nf, nf // 500)] = np.nan
+    dt = 0.9
+    v = faces(pg, g, vel)
+    out = faces(pg, g, np.zeros(nf, np.float32))
+    pg.advect_mac(out, v, dt, v)
+    same(host(out), oracle.advect_mac(vel, dt, vel, dims))
+
+
 def test_advection_nonfinite(pg, oracle):
     """NaN / inf velocities follow the reference's f64::max/min rules."""
     dims = (9, 11)
