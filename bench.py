@@ -607,6 +607,16 @@ def ours(args, spec, dims):
         lib.pg_profile_read_active(k, C.byref(t), C.byref(n))
         if n.value:
             kinds[lib.pg_profile_kind_name(k).decode()] = (t.value, n.value)
+    # --- one V-cycle and its coarse levels, replayed as CUDA graphs --------
+    vcyc = None
+    if mg:
+        full_ms, coarse_ms = C.c_double(), C.c_double()
+        if lib.pg_debug_mg_vcycle_ms(grid.handle, C.c_double(spec["dt"]), 2, 50, C.byref(full_ms),
+                                     C.byref(coarse_ms)) == N.PG_OK:
+            per_step = float(np.mean(its))  # one V-cycle per CG iteration
+            vcyc = {"full_ms": full_ms.value, "coarse_ms": coarse_ms.value, "vcycles_per_step": per_step,
+                    "coarse_ms_per_step": coarse_ms.value * per_step,
+                    "how": "each captured once into a CUDA graph and replayed 50 times between two events"}
     # --- plain FP32 PCG on the same workload -------------------------------
     plain_out = None
     if not args.no_plain:
@@ -671,6 +681,7 @@ def ours(args, spec, dims):
             "roofline": roof,
             "profiled_ms_per_step": ms_prof / args.steps,
             "kernels_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in sorted(kinds.items(), key=lambda kv: -kv[1][0])},
+            "mg_vcycle_graph": vcyc,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
         }
         print(json.dumps(out), flush=True)

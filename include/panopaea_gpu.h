@@ -488,6 +488,13 @@ int pg_profile_read_active(int kind, double* total_ms, int64_t* launches);
 int pg_debug_set_stage_wait_polls(uint32_t polls);
 uint32_t pg_debug_stage_wait_polls_default(void);
 
+/* Diagnostic (no reference counterpart): average device time (ms) of one
+ * multigrid V-cycle of the grid's hierarchy for dt with nsmooth sweeps, and
+ * of its coarse part (every level below the fine one), each captured once
+ * into a CUDA graph and replayed `reps` times on a private stream with r = 0.
+ * Needs at least two levels; synchronous. */
+int pg_debug_mg_vcycle_ms(pg_grid* g, double dt, int nsmooth, int reps, double* full_ms, double* coarse_ms);
+
 #ifdef __cplusplus
 }
 #endif

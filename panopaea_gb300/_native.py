@@ -102,6 +102,8 @@ _SIGS = {
     "pg_status_string": (C.c_char_p, [_I]),
     "pg_debug_set_stage_wait_polls": (_I, [C.c_uint32]),
     "pg_debug_stage_wait_polls_default": (C.c_uint32, []),
+    "pg_debug_mg_vcycle_ms": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]),
     "pg_last_error": (C.c_char_p, []),
     "pg_version": (_I, []),
     "pg_grid_create_2d": (_I, [_I64, _I64, C.POINTER(_P)]),

@@ -59,6 +59,10 @@ struct MgHierarchy {
     uint64_t id = 0;  // unique per build (CUDA-graph cache key)
     Pockets pockets;  // fluid components (empty when the fluid is connected)
     int tail = 0;     // first level handled by the single-block tail kernel (nlev: none)
+    int ct_lt = 0;    // cluster tail (3D): first level (0: not used), first rank-0 level, ranks
+    int ct_ls = 0;
+    int ct_ranks = 0;
+    size_t ct_smem = 0;
     double nfluid = 0;  // cells with an open face (the lazy projection's count)
     // fine level of 3D grids: fused red-black pairs (k_mg_pair) ping-pong
     // between z and e0b; tensor maps of the flags and of the vectors met
@@ -470,7 +474,7 @@ __global__ void __launch_bounds__(kPThreads, kPMinBlocks)
 // columns); fine plane p is staged with e (one-cell halo), f and the flags
 // into a kQStages-deep ring, and coarse plane Z reads the stages of fine
 // planes 2Z-1 .. 2Z+2.  Each thread sums its eight children's residuals
-// f - A e in the order and with the arithmetic of k_mg_restrict<true>
+// f - A e in the order and with the arithmetic of k_mg_restrict8<true>
 // (bit-identical).  Per fine cell: 4 bytes of e (+ halo), 4 of f, 1 of flags
 // in; 0.5 of the coarse right-hand side out.
 constexpr int kQX = 64, kQY = 16, kQThreads = (kQX / 2) * (kQY / 2);
@@ -615,38 +619,54 @@ static int restrict_cap(const pg_grid* g) {
     return cap;
 }
 
-// Residual of level l restricted (summed over children) to level l+1.
+// Residual of level l restricted (summed over children) to level l+1, one
+// thread per child: eight lanes of a warp form the eight child residuals of
+// one coarse cell (those that exist), and the first of them sums them in
+// (z, y, x) order.
 template <bool L0>
 __global__ void __launch_bounds__(kMgThreads)
-    k_mg_restrict(LV v, const float* __restrict__ e, const float* __restrict__ f, float* __restrict__ fc, int cd,
-                  int ch, int cw, CgState* st) {
+    k_mg_restrict8(LV v, const float* __restrict__ e, const float* __restrict__ f, float* __restrict__ fc, int cd,
+                   int ch, int cw, CgState* st) {
     if (st->done) return;
     const int hw = v.h * v.w;
     const int nc = cd * ch * cw;
-    for (int C = blockIdx.x * blockDim.x + threadIdx.x; C < nc; C += gridDim.x * blockDim.x) {
-        const int CZY = C / cw, X = C - CZY * cw;
-        const int Z = CZY / ch, Y = CZY - Z * ch;
-        float sum = 0.f;
-        const int z1 = v.nd == 3 ? min(2 * Z + 2, v.d) : 1;
-        const int y1 = min(2 * Y + 2, v.h), x1 = min(2 * X + 2, v.w);
-        for (int z = (v.nd == 3 ? 2 * Z : 0); z < z1; ++z)
-            for (int y = 2 * Y; y < y1; ++y)
-                for (int x = 2 * X; x < x1; ++x) {
-                    const int c = (z * v.h + y) * v.w + x;
-                    const Cell<L0> cl(v, c, z, y, x);
-                    const float ecv = e[c];
-                    float a = 0.f;
-                    if (cl.wxl != 0.f) a += cl.wxl * (ecv - e[c - 1]);
-                    if (cl.wxh != 0.f) a += cl.wxh * (ecv - e[c + 1]);
-                    if (cl.wyl != 0.f) a += cl.wyl * (ecv - e[c - v.w]);
-                    if (cl.wyh != 0.f) a += cl.wyh * (ecv - e[c + v.w]);
-                    if (v.nd == 3) {
-                        if (cl.wzl != 0.f) a += cl.wzl * (ecv - e[c - hw]);
-                        if (cl.wzh != 0.f) a += cl.wzh * (ecv - e[c + hw]);
-                    }
-                    sum += f[c] - a;
+    const unsigned lane = threadIdx.x & 31, grp = lane & ~7u;
+    // every lane of a warp runs the same number of trips (shuffles below)
+    const int n8 = (nc * 8 + 31) & ~31;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n8; t += gridDim.x * blockDim.x) {
+        const int C = t >> 3, j = t & 7;
+        float term = 0.f;
+        bool has = false;
+        if (C < nc) {
+            const int CZY = C / cw, X = C - CZY * cw;
+            const int Z = CZY / ch, Y = CZY - Z * ch;
+            const int z = (v.nd == 3 ? 2 * Z : 0) + (j >> 2), y = 2 * Y + ((j >> 1) & 1), x = 2 * X + (j & 1);
+            const int z1 = v.nd == 3 ? min(2 * Z + 2, v.d) : 1;
+            if (z < z1 && y < v.h && x < v.w) {
+                const int c = (z * v.h + y) * v.w + x;
+                const Cell<L0> cl(v, c, z, y, x);
+                const float ecv = e[c];
+                float a = 0.f;
+                if (cl.wxl != 0.f) a += cl.wxl * (ecv - e[c - 1]);
+                if (cl.wxh != 0.f) a += cl.wxh * (ecv - e[c + 1]);
+                if (cl.wyl != 0.f) a += cl.wyl * (ecv - e[c - v.w]);
+                if (cl.wyh != 0.f) a += cl.wyh * (ecv - e[c + v.w]);
+                if (v.nd == 3) {
+                    if (cl.wzl != 0.f) a += cl.wzl * (ecv - e[c - hw]);
+                    if (cl.wzh != 0.f) a += cl.wzh * (ecv - e[c + hw]);
                 }
-        fc[C] = sum;
+                term = f[c] - a;
+                has = true;
+            }
+        }
+        const unsigned valid = __ballot_sync(0xffffffffu, has);
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float tk = __shfl_sync(0xffffffffu, term, grp + k);
+            if ((valid >> (grp + k)) & 1u) sum += tk;
+        }
+        if (j == 0 && C < nc) fc[C] = sum;
     }
 }
 
@@ -713,64 +733,129 @@ struct TailArgs {
     TailLevel L[kMaxLevels];
 };
 
-template <int MODE>
+// One half-sweep by the whole block, or (WARP) by warp 0 alone.
+// Every value a cell may need is loaded before any is used (a missing
+// neighbour's offset is clamped to the cell itself and its value ignored),
+// so a cell waits for one round of shared-memory loads; the arithmetic is
+// that of k_mg_smooth.
+template <int MODE, bool WARP = false>
 __device__ __forceinline__ void tail_smooth(const LV& v, float* e, const float* f, const float* ec, int cw, int ch,
                                             int color) {
     const int hw = v.h * v.w, half = (v.w + 1) >> 1, total = v.d * v.h * half;
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int t0 = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x, dt = WARP ? 32 : (int)blockDim.x;
+    const bool d3 = v.nd == 3;
+    for (int i = t0; i < total; i += dt) {
         const int row = i / half, k2 = i - row * half;
         const int z = row / v.h, y = row - z * v.h;
         const int x = 2 * k2 + ((y + z + color) & 1);
         if (x >= v.w) continue;
         const int c = row * v.w + x;
-        const Cell<false> cl(v, c, z, y, x);
+        const bool hx = x + 1 < v.w, hy = y + 1 < v.h, hz = d3 && z + 1 < v.d;
+        const int ox0 = x > 0 ? -1 : 0, ox1 = hx ? 1 : 0, oy0 = y > 0 ? -v.w : 0, oy1 = hy ? v.w : 0;
+        const int oz0 = d3 && z > 0 ? -hw : 0, oz1 = hz ? hw : 0;
+        const float wxl = v.wx[c], wxh_ = v.wx[c + ox1], wyl = v.wy[c], wyh_ = v.wy[c + oy1];
+        const float wzl = d3 ? v.wz[c] : 0.f, wzh_ = v.wz[c + oz1];
+        const float inv = v.invd[c];
         float s = f[c];
         if (MODE == NB_SELF) {
-            e[c] = s * cl.inv;
+            e[c] = s * inv;
             continue;
         }
-        if (cl.wxl != 0.f) s += cl.wxl * nbval<false, MODE>(v, e, f, ec, cw, ch, c - 1, z, y, x - 1);
-        if (cl.wxh != 0.f) s += cl.wxh * nbval<false, MODE>(v, e, f, ec, cw, ch, c + 1, z, y, x + 1);
-        if (cl.wyl != 0.f) s += cl.wyl * nbval<false, MODE>(v, e, f, ec, cw, ch, c - v.w, z, y - 1, x);
-        if (cl.wyh != 0.f) s += cl.wyh * nbval<false, MODE>(v, e, f, ec, cw, ch, c + v.w, z, y + 1, x);
-        if (v.nd == 3) {
-            if (cl.wzl != 0.f) s += cl.wzl * nbval<false, MODE>(v, e, f, ec, cw, ch, c - hw, z - 1, y, x);
-            if (cl.wzh != 0.f) s += cl.wzh * nbval<false, MODE>(v, e, f, ec, cw, ch, c + hw, z + 1, y, x);
+        const float n0 = nbval<false, MODE>(v, e, f, ec, cw, ch, c + ox0, z, y, x + (x > 0 ? -1 : 0));
+        const float n1 = nbval<false, MODE>(v, e, f, ec, cw, ch, c + ox1, z, y, x + ox1);
+        const float n2 = nbval<false, MODE>(v, e, f, ec, cw, ch, c + oy0, z, y + (y > 0 ? -1 : 0), x);
+        const float n3 = nbval<false, MODE>(v, e, f, ec, cw, ch, c + oy1, z, y + (hy ? 1 : 0), x);
+        const float n4 = nbval<false, MODE>(v, e, f, ec, cw, ch, c + oz0, z + (oz0 ? -1 : 0), y, x);
+        const float n5 = nbval<false, MODE>(v, e, f, ec, cw, ch, c + oz1, z + (hz ? 1 : 0), y, x);
+        const float wxh = hx ? wxh_ : 0.f, wyh = hy ? wyh_ : 0.f, wzh = hz ? wzh_ : 0.f;
+        if (wxl != 0.f) s += wxl * n0;
+        if (wxh != 0.f) s += wxh * n1;
+        if (wyl != 0.f) s += wyl * n2;
+        if (wyh != 0.f) s += wyh * n3;
+        if (d3) {
+            if (wzl != 0.f) s += wzl * n4;
+            if (wzh != 0.f) s += wzh * n5;
         }
-        e[c] = s * cl.inv;
+        e[c] = s * inv;
+    }
+    if (WARP)
+        __syncwarp();
+    else
+        __syncthreads();
+}
+
+// The restriction of k_mg_restrict8 inside one block: one thread per child,
+// eight lanes per coarse cell, summed by the first in (z, y, x) order.
+__device__ __forceinline__ void tail_restrict(const LV& v, const float* e, const float* f, float* fc, int cd, int ch,
+                                              int cw) {
+    const int hw = v.h * v.w, nc = cd * ch * cw;
+    const bool d3 = v.nd == 3;
+    const unsigned lane = threadIdx.x & 31, grp = lane & ~7u;
+    const int n8 = (nc * 8 + 31) & ~31;  // whole warps: every lane runs the same trips
+    for (int t = threadIdx.x; t < n8; t += blockDim.x) {
+        const int C = t >> 3, j = t & 7;
+        const int CZY = C / cw, X = C - CZY * cw;
+        const int Z = CZY / ch, Y = CZY - Z * ch;
+        const int z = (d3 ? 2 * Z : 0) + (j >> 2), y = 2 * Y + ((j >> 1) & 1), x = 2 * X + (j & 1);
+        const bool has = C < nc && z < (d3 ? v.d : 1) && y < v.h && x < v.w;
+        float term = 0.f;
+        if (has) {
+            const int c = (z * v.h + y) * v.w + x;
+            const bool hx = x + 1 < v.w, hy = y + 1 < v.h, hz = d3 && z + 1 < v.d;
+            const int ox0 = x > 0 ? -1 : 0, ox1 = hx ? 1 : 0, oy0 = y > 0 ? -v.w : 0, oy1 = hy ? v.w : 0;
+            const int oz0 = d3 && z > 0 ? -hw : 0, oz1 = hz ? hw : 0;
+            const float wxl = v.wx[c], wxh_ = v.wx[c + ox1], wyl = v.wy[c], wyh_ = v.wy[c + oy1];
+            const float wzl = d3 ? v.wz[c] : 0.f, wzh_ = v.wz[c + oz1];
+            const float ecv = e[c], e0 = e[c + ox0], e1 = e[c + ox1], e2 = e[c + oy0], e3 = e[c + oy1],
+                        e4 = e[c + oz0], e5 = e[c + oz1], fv = f[c];
+            const float wxh = hx ? wxh_ : 0.f, wyh = hy ? wyh_ : 0.f, wzh = hz ? wzh_ : 0.f;
+            float a = 0.f;
+            if (wxl != 0.f) a += wxl * (ecv - e0);
+            if (wxh != 0.f) a += wxh * (ecv - e1);
+            if (wyl != 0.f) a += wyl * (ecv - e2);
+            if (wyh != 0.f) a += wyh * (ecv - e3);
+            if (d3) {
+                if (wzl != 0.f) a += wzl * (ecv - e4);
+                if (wzh != 0.f) a += wzh * (ecv - e5);
+            }
+            term = fv - a;
+        }
+        const unsigned valid = __ballot_sync(0xffffffffu, has);
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float tk = __shfl_sync(0xffffffffu, term, grp + k);
+            if ((valid >> (grp + k)) & 1u) sum += tk;
+        }
+        if (j == 0 && C < nc) fc[C] = sum;
     }
     __syncthreads();
 }
 
-__device__ __forceinline__ void tail_restrict(const LV& v, const float* e, const float* f, float* fc, int cd, int ch,
-                                              int cw) {
-    const int hw = v.h * v.w, nc = cd * ch * cw;
-    for (int C = threadIdx.x; C < nc; C += blockDim.x) {
-        const int CZY = C / cw, X = C - CZY * cw;
-        const int Z = CZY / ch, Y = CZY - Z * ch;
-        float sum = 0.f;
-        const int z1 = v.nd == 3 ? min(2 * Z + 2, v.d) : 1;
-        const int y1 = min(2 * Y + 2, v.h), x1 = min(2 * X + 2, v.w);
-        for (int z = (v.nd == 3 ? 2 * Z : 0); z < z1; ++z)
-            for (int y = 2 * Y; y < y1; ++y)
-                for (int x = 2 * X; x < x1; ++x) {
-                    const int c = (z * v.h + y) * v.w + x;
-                    const Cell<false> cl(v, c, z, y, x);
-                    const float ecv = e[c];
-                    float a = 0.f;
-                    if (cl.wxl != 0.f) a += cl.wxl * (ecv - e[c - 1]);
-                    if (cl.wxh != 0.f) a += cl.wxh * (ecv - e[c + 1]);
-                    if (cl.wyl != 0.f) a += cl.wyl * (ecv - e[c - v.w]);
-                    if (cl.wyh != 0.f) a += cl.wyh * (ecv - e[c + v.w]);
-                    if (v.nd == 3) {
-                        if (cl.wzl != 0.f) a += cl.wzl * (ecv - e[c - hw]);
-                        if (cl.wzh != 0.f) a += cl.wzh * (ecv - e[c + hw]);
-                    }
-                    sum += f[c] - a;
-                }
-        fc[C] = sum;
+// Coarsest level: symmetric red-black Gauss-Seidel from e = 0 (`pairs`
+// (red, black) sweeps, then `pairs` (black, red)); a level of at most 256
+// cells is swept by warp 0 alone, with warp barriers.
+__device__ __forceinline__ void tail_coarsest(const LV& cv, float* e, const float* f) {
+    const int n = cv.d * cv.h * cv.w;
+    const int pairs = coarse_pairs(cv.d, cv.h, cv.w);
+    if (n <= 256) {
+        if (threadIdx.x < 32) {
+            for (int c = threadIdx.x; c < n; c += 32) e[c] = 0.f;
+            __syncwarp();
+            for (int it = 0; it < 4 * pairs; ++it) {
+                const int color = it < 2 * pairs ? (it & 1) : ((it & 1) ^ 1);
+                tail_smooth<NB_PLAIN, true>(cv, e, f, nullptr, 1, 1, color);
+            }
+        }
+        __syncthreads();
+        return;
     }
+    for (int c = threadIdx.x; c < n; c += blockDim.x) e[c] = 0.f;
     __syncthreads();
+    for (int it = 0; it < 4 * pairs; ++it) {
+        const int color = it < 2 * pairs ? (it & 1) : ((it & 1) ^ 1);
+        tail_smooth<NB_PLAIN>(cv, e, f, nullptr, 1, 1, color);
+    }
 }
 
 constexpr int kTailThreads = 1024;
@@ -835,20 +920,7 @@ __device__ __forceinline__ void tail_body(const TailArgs& A, float* tsm) {
         }
         tail_restrict(v, e, f, F(l + 1), c.d, c.h, c.w);
     }
-    // coarsest: symmetric red-black Gauss-Seidel from e = 0
-    {
-        const LV cv = lv(nl - 1);
-        float* e = E(nl - 1);
-        const float* f = F(nl - 1);
-        const int n = cv.d * cv.h * cv.w;
-        for (int c = threadIdx.x; c < n; c += blockDim.x) e[c] = 0.f;
-        __syncthreads();
-        const int pairs = coarse_pairs(cv.d, cv.h, cv.w);
-        for (int it = 0; it < 4 * pairs; ++it) {
-            const int color = it < 2 * pairs ? (it & 1) : ((it & 1) ^ 1);
-            tail_smooth<NB_PLAIN>(cv, e, f, nullptr, 1, 1, color);
-        }
-    }
+    tail_coarsest(lv(nl - 1), E(nl - 1), F(nl - 1));
     // up
     for (int l = nl - 2; l >= A.lt; --l) {
         const TailLevel& c = A.L[l + 1];
@@ -870,6 +942,284 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs A, CgState* s
     if (st->done) return;
     extern __shared__ float tsm[];
     tail_body(A, tsm);
+}
+
+// ---------------------------------------------------------------------------
+// Cluster tail (3D): the levels from the first one of at most kCtCells cells
+// down to the coarsest, in ONE thread-block cluster of R blocks (16 where the
+// device allows it, else 8).  Levels larger than kCtLocal cells are cut into
+// z slabs of ppc = ceil(d / R) planes, one per rank, each rank holding its
+// slab of wx, wy, wz, 1/diag, e and f in shared memory; a rank updates its own
+// cells and reads the neighbouring planes of other ranks through distributed
+// shared memory, with a cluster barrier between half-sweeps.  Smaller levels
+// live in rank 0 alone and run the single-block tail's phases with block
+// barriers.  Every cell is computed by the same formula, in the same order of
+// operations, as k_mg_smooth / k_mg_restrict8 / the single-block tail, so the
+// V-cycle is bit-identical to the per-level kernels plus k_mg_tail.
+
+constexpr int kCtThreads = 1024;
+constexpr int kCtCells = 32768;  // first level of the cluster tail: at most this many cells
+constexpr int kCtLocal = 512;    // levels at most this large live in rank 0 alone
+constexpr int kCtMaxRanks = 16;
+constexpr int kCtSmemMax = 200 * 1024;
+
+struct CtLevel {
+    int d, h, w;
+    int ppc;  // planes per rank (d: the level lives in rank 0)
+    int off;  // offset (floats) of the level's block [wx | wy | wz | invd | e | f] in shared memory
+    int P;    // floats per array of the block: ppc * h * w
+    const float* wx;
+    const float* wy;
+    const float* wz;
+    const float* invd;
+};
+
+struct CtArgs {
+    int lt, ls, nl, nsmooth, ranks;
+    float* e_out;       // global e of level lt
+    const float* f_in;  // global f of level lt
+    CtLevel L[kMaxLevels];
+};
+
+__device__ __forceinline__ unsigned ct_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ float* ct_map(float* p, unsigned rank) {
+    unsigned long long r;
+    asm volatile("mapa.u64 %0, %1, %2;" : "=l"(r) : "l"(p), "r"(rank));
+    return (float*)r;
+}
+
+__device__ __forceinline__ void ct_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Array 0 (wx) of level L at plane z, on the rank that owns it.
+__device__ __forceinline__ float* ct_plane(float* const* peer, const CtLevel& L, int z) {
+    const int r = z / L.ppc;
+    return peer[r] + L.off + (z - r * L.ppc) * L.h * L.w;
+}
+
+// Neighbour value of the smoother at the cell whose array-0 entry is q
+// (z, y, x): e, f / diag (first half-sweep from e = 0) or e + the coarse
+// correction of its parent (first post-smoothing half-sweep).
+template <int MODE>
+__device__ __forceinline__ float ct_nb(float* const* peer, const float* q, int P, const CtLevel* Lc, int z, int y,
+                                       int x) {
+    if (MODE == NB_FIRST) return q[5 * P] * q[3 * P];
+    if (MODE == NB_PROLONG) {
+        const float* pc = ct_plane(peer, *Lc, z >> 1) + 4 * Lc->P + (y >> 1) * Lc->w + (x >> 1);
+        return q[4 * P] + *pc;
+    }
+    return q[4 * P];
+}
+
+// One half-sweep of a distributed level over the calling rank's planes.
+// Every value a cell may need is loaded before any is used (a missing
+// neighbour's offset is clamped to the cell itself and its value ignored),
+// so a cell waits for one round of shared and distributed-shared loads.
+template <int MODE>
+__device__ void ct_smooth(float* const* peer, const CtLevel& L, const CtLevel* Lc, int rank, int color) {
+    const int h = L.h, w = L.w, P = L.P;
+    const int z0 = rank * L.ppc, nz = max(0, min(L.ppc, L.d - z0));
+    const int half = (w + 1) >> 1, total = nz * h * half;
+    float* B = peer[rank] + L.off;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        const int row = i / half, k2 = i - row * half;
+        const int zl = row / h, y = row - zl * h, z = z0 + zl;
+        const int x = 2 * k2 + ((y + z + color) & 1);
+        if (x >= w) continue;
+        const int c = row * w + x;
+        const float* q = B + c;
+        const bool hx = x + 1 < w, hy = y + 1 < h, hz = z + 1 < L.d;
+        const int ox0 = x > 0 ? -1 : 0, ox1 = hx ? 1 : 0, oy0 = y > 0 ? -w : 0, oy1 = hy ? w : 0;
+        const float* qd = z > 0 ? (zl > 0 ? q - h * w : ct_plane(peer, L, z - 1) + y * w + x) : q;
+        const float* qu = hz ? (zl + 1 < L.ppc ? q + h * w : ct_plane(peer, L, z + 1) + y * w + x) : q;
+        const float wxl = q[0], wxh_ = q[ox1], wyl = q[P], wyh_ = q[P + oy1], wzl = q[2 * P], wzh_ = qu[2 * P];
+        const float inv = q[3 * P];
+        float s = q[5 * P];
+        if (MODE == NB_SELF) {
+            B[4 * P + c] = s * inv;
+            continue;
+        }
+        const float n0 = ct_nb<MODE>(peer, q + ox0, P, Lc, z, y, x + (x > 0 ? -1 : 0));
+        const float n1 = ct_nb<MODE>(peer, q + ox1, P, Lc, z, y, x + ox1);
+        const float n2 = ct_nb<MODE>(peer, q + oy0, P, Lc, z, y + (y > 0 ? -1 : 0), x);
+        const float n3 = ct_nb<MODE>(peer, q + oy1, P, Lc, z, y + (hy ? 1 : 0), x);
+        const float n4 = ct_nb<MODE>(peer, qd, P, Lc, z > 0 ? z - 1 : z, y, x);
+        const float n5 = ct_nb<MODE>(peer, qu, P, Lc, hz ? z + 1 : z, y, x);
+        const float wxh = hx ? wxh_ : 0.f, wyh = hy ? wyh_ : 0.f, wzh = hz ? wzh_ : 0.f;
+        if (wxl != 0.f) s += wxl * n0;
+        if (wxh != 0.f) s += wxh * n1;
+        if (wyl != 0.f) s += wyl * n2;
+        if (wyh != 0.f) s += wyh * n3;
+        if (wzl != 0.f) s += wzl * n4;
+        if (wzh != 0.f) s += wzh * n5;
+        B[4 * P + c] = s * inv;
+    }
+}
+
+// Residual of distributed level L summed over children into f of level Lc,
+// one thread per child (eight lanes per coarse cell, summed by the first in
+// (z, y, x) order as k_mg_restrict8 does).  Coarse plane Z is computed by the
+// rank owning fine plane 2Z.
+__device__ void ct_restrict(float* const* peer, const CtLevel& L, const CtLevel& Lc, int rank) {
+    const int h = L.h, w = L.w, P = L.P;
+    const int ch = Lc.h, cw = Lc.w, chw = ch * cw;
+    // coarse planes Z with 2Z in [rank * ppc, (rank + 1) * ppc)
+    const int Z0 = (rank * L.ppc + 1) / 2, Z1 = min(Lc.d, ((rank + 1) * L.ppc + 1) / 2);
+    const int total = max(0, Z1 - Z0) * chw;
+    const unsigned lane = threadIdx.x & 31, grp = lane & ~7u;
+    const int n8 = (total * 8 + 31) & ~31;  // whole warps: every lane runs the same trips
+    for (int t = threadIdx.x; t < n8; t += blockDim.x) {
+        const int i = t >> 3, j = t & 7;
+        const int Z = Z0 + i / chw, YX = i - (i / chw) * chw;
+        const int Y = YX / cw, X = YX - Y * cw;
+        const int z = 2 * Z + (j >> 2), y = 2 * Y + ((j >> 1) & 1), x = 2 * X + (j & 1);
+        const bool has = i < total && z < L.d && y < h && x < w;
+        float term = 0.f;
+        if (has) {
+            const int k = y * w + x;
+            const float* q = ct_plane(peer, L, z) + k;
+            const bool hx = x + 1 < w, hy = y + 1 < h, hz = z + 1 < L.d;
+            const int ox0 = x > 0 ? -1 : 0, ox1 = hx ? 1 : 0, oy0 = y > 0 ? -w : 0, oy1 = hy ? w : 0;
+            const float* pd = z > 0 ? ct_plane(peer, L, z - 1) + k : q;
+            const float* pu = hz ? ct_plane(peer, L, z + 1) + k : q;
+            const float wxl = q[0], wxh_ = q[ox1], wyl = q[P], wyh_ = q[P + oy1], wzl = q[2 * P], wzh_ = pu[2 * P];
+            const float ecv = q[4 * P], e0 = q[4 * P + ox0], e1 = q[4 * P + ox1], e2 = q[4 * P + oy0],
+                        e3 = q[4 * P + oy1], e4 = pd[4 * P], e5 = pu[4 * P], fv = q[5 * P];
+            const float wxh = hx ? wxh_ : 0.f, wyh = hy ? wyh_ : 0.f, wzh = hz ? wzh_ : 0.f;
+            float a = 0.f;
+            if (wxl != 0.f) a += wxl * (ecv - e0);
+            if (wxh != 0.f) a += wxh * (ecv - e1);
+            if (wyl != 0.f) a += wyl * (ecv - e2);
+            if (wyh != 0.f) a += wyh * (ecv - e3);
+            if (wzl != 0.f) a += wzl * (ecv - e4);
+            if (wzh != 0.f) a += wzh * (ecv - e5);
+            term = fv - a;
+        }
+        const unsigned valid = __ballot_sync(0xffffffffu, has);
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float tk = __shfl_sync(0xffffffffu, term, grp + k);
+            if ((valid >> (grp + k)) & 1u) sum += tk;
+        }
+        if (j == 0 && i < total) ct_plane(peer, Lc, Z)[5 * Lc.P + YX] = sum;
+    }
+}
+
+__global__ void __launch_bounds__(kCtThreads) k_mg_ctail(CtArgs A, CgState* st) {
+    if (st->done) return;  // the same value in every block of the cluster
+    extern __shared__ float csm[];
+    __shared__ float* peer[kCtMaxRanks];
+    const int rank = (int)ct_rank();
+    if (threadIdx.x < A.ranks) peer[threadIdx.x] = ct_map(csm, threadIdx.x);
+    __syncthreads();
+    const int lt = A.lt, ls = A.ls, nl = A.nl, ns = A.nsmooth;
+    // load: the distributed levels' slabs, and rank 0's levels
+    for (int l = lt; l < nl; ++l) {
+        const CtLevel& L = A.L[l];
+        const int z0 = l < ls ? rank * L.ppc : 0;
+        const int nz = l < ls ? max(0, min(L.ppc, L.d - z0)) : (rank == 0 ? L.d : 0);
+        const int n = nz * L.h * L.w, g0 = z0 * L.h * L.w;
+        float* B = csm + L.off;
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            B[c] = L.wx[g0 + c];
+            B[L.P + c] = L.wy[g0 + c];
+            B[2 * L.P + c] = L.wz[g0 + c];
+            B[3 * L.P + c] = L.invd[g0 + c];
+            if (l == lt) B[5 * L.P + c] = A.f_in[g0 + c];
+        }
+    }
+    ct_sync();
+    // down through the distributed levels
+    for (int l = lt; l < ls; ++l) {
+        const CtLevel& L = A.L[l];
+        ct_smooth<NB_FIRST>(peer, L, nullptr, rank, 1);
+        ct_sync();
+        if (ns == 1) {
+            ct_smooth<NB_SELF>(peer, L, nullptr, rank, 0);
+            ct_sync();
+        }
+        for (int k = 1; k < ns; ++k) {
+            ct_smooth<NB_PLAIN>(peer, L, nullptr, rank, 0);
+            ct_sync();
+            ct_smooth<NB_PLAIN>(peer, L, nullptr, rank, 1);
+            ct_sync();
+        }
+        ct_restrict(peer, L, A.L[l + 1], rank);
+        ct_sync();
+    }
+    // rank 0: levels [ls, nl) as in the single-block tail
+    if (rank == 0) {
+        auto lv = [&](int l) -> LV {
+            const CtLevel& T = A.L[l];
+            float* p = csm + T.off;
+            LV v;
+            v.nd = 3;
+            v.d = T.d;
+            v.h = T.h;
+            v.w = T.w;
+            v.flags = nullptr;
+            v.wx = p;
+            v.wy = p + T.P;
+            v.wz = p + 2 * T.P;
+            v.invd = p + 3 * T.P;
+            v.dt = 0.f;
+            return v;
+        };
+        auto E = [&](int l) -> float* { return csm + A.L[l].off + 4 * A.L[l].P; };
+        auto F = [&](int l) -> float* { return csm + A.L[l].off + 5 * A.L[l].P; };
+        for (int l = ls; l + 1 < nl; ++l) {
+            const CtLevel& c = A.L[l + 1];
+            const LV v = lv(l);
+            float* e = E(l);
+            const float* f = F(l);
+            tail_smooth<NB_FIRST>(v, e, f, nullptr, c.w, c.h, 1);
+            if (ns == 1) tail_smooth<NB_SELF>(v, e, f, nullptr, c.w, c.h, 0);
+            for (int k = 1; k < ns; ++k) {
+                tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 0);
+                tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 1);
+            }
+            tail_restrict(v, e, f, F(l + 1), c.d, c.h, c.w);
+        }
+        tail_coarsest(lv(nl - 1), E(nl - 1), F(nl - 1));
+        for (int l = nl - 2; l >= ls; --l) {
+            const CtLevel& c = A.L[l + 1];
+            const LV v = lv(l);
+            float* e = E(l);
+            const float* f = F(l);
+            tail_smooth<NB_PROLONG>(v, e, f, E(l + 1), c.w, c.h, 1);
+            for (int k = 0; k < ns; ++k) {
+                if (k > 0) tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 1);
+                tail_smooth<NB_PLAIN>(v, e, f, nullptr, c.w, c.h, 0);
+            }
+        }
+    }
+    ct_sync();
+    // up through the distributed levels
+    for (int l = ls - 1; l >= lt; --l) {
+        const CtLevel& L = A.L[l];
+        ct_smooth<NB_PROLONG>(peer, L, &A.L[l + 1], rank, 1);
+        ct_sync();
+        for (int k = 0; k < ns; ++k) {
+            if (k > 0) {
+                ct_smooth<NB_PLAIN>(peer, L, nullptr, rank, 1);
+                ct_sync();
+            }
+            ct_smooth<NB_PLAIN>(peer, L, nullptr, rank, 0);
+            ct_sync();
+        }
+    }
+    // level lt's correction to global memory (own slab, own shared memory)
+    const CtLevel& L = A.L[lt];
+    const int z0 = rank * L.ppc, nz = max(0, min(L.ppc, L.d - z0));
+    const float* Eo = csm + L.off + 4 * L.P;
+    for (int c = threadIdx.x; c < nz * L.h * L.w; c += blockDim.x) A.e_out[z0 * L.h * L.w + c] = Eo[c];
 }
 
 // Coarse face weights: half the sum of the fine weights on the coarse face.
@@ -945,6 +1295,7 @@ void release_mg(Extras* ex) {
 static int blocks_for(const pg_grid* g, i64 n) { return grid_blocks(g, n, kMgThreads, 8); }
 
 static int pair_setup(pg_grid* g, MgHierarchy* H);
+static void ctail_setup(MgHierarchy* H);
 
 // (Re)build the hierarchy for the grid's current mask and dt.
 static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
@@ -1036,6 +1387,7 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
         int prc = upload_pockets(cells, start, &H->pockets);
         if (prc) return prc;
     }
+    ctail_setup(H);
     // coarse operators
     cudaStream_t s = g->stream;
     for (int l = 0; l + 1 < nl; ++l) {
@@ -1229,6 +1581,112 @@ static int launch_tail(pg_grid* g, const MgHierarchy& H, int nsmooth) {
     return PG_OK;
 }
 
+// Shared-memory layout of the cluster tail with R ranks; 0 when it does not
+// fit.
+static size_t ctail_layout(const MgHierarchy& H, int lt, int ls, int R, CtArgs* A) {
+    size_t off = 0;
+    for (int l = lt; l < H.nlev; ++l) {
+        const Dims& D = H.lv[l].D;
+        CtLevel& L = A->L[l];
+        L.d = (int)D.d;
+        L.h = (int)D.h;
+        L.w = (int)D.w;
+        L.ppc = l < ls ? (int)((D.d + R - 1) / R) : (int)D.d;
+        L.P = (int)(((size_t)L.ppc * D.h * D.w + 3) & ~(size_t)3);
+        L.off = (int)off;
+        L.wx = H.lv[l].wx;
+        L.wy = H.lv[l].wy;
+        L.wz = H.lv[l].wz;
+        L.invd = H.lv[l].invd;
+        off += 6 * (size_t)L.P;
+    }
+    const size_t bytes = off * sizeof(float);
+    return bytes <= (size_t)kCtSmemMax ? bytes : 0;
+}
+
+static cudaLaunchConfig_t ctail_config(int R, size_t smem, cudaStream_t s, cudaLaunchAttribute* at) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(R, 1, 1);
+    cfg.blockDim = dim3(kCtThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = R;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+// Cluster tail for 3D hierarchies: a level of at most kCtCells cells above
+// the rank-0 levels, 16 or 8 ranks that fit and can be resident together;
+// PG_MG_CTAIL=0 keeps the per-level kernels and the single-block tail (a
+// diagnostic switch read per build).
+static void ctail_setup(MgHierarchy* H) {
+    H->ct_lt = 0;
+    const char* env = getenv("PG_MG_CTAIL");
+    if ((env && env[0] == '0') || H->D0.nd != 3) return;
+    const int nl = H->nlev;
+    int lt = 0, ls = 0;
+    for (int l = 1; l < nl; ++l)
+        if (H->lv[l].D.nc() <= kCtCells) {
+            lt = l;
+            break;
+        }
+    if (lt == 0) return;
+    for (int l = lt; l < nl; ++l)
+        if (H->lv[l].D.nc() <= kCtLocal) {
+            ls = l;
+            break;
+        }
+    if (ls <= lt || ls > nl - 1) return;
+    const char* renv = getenv("PG_MG_CTAIL_RANKS");
+    const int only = renv ? atoi(renv) : 0;
+    for (int R : {16, 8}) {
+        if (only && R != only) continue;
+        CtArgs A{};
+        const size_t smem = ctail_layout(*H, lt, ls, R, &A);
+        if (smem == 0) continue;
+        if (cudaFuncSetAttribute(k_mg_ctail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            (R > 8 && cudaFuncSetAttribute(k_mg_ctail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                          cudaSuccess)) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchAttribute at[1];
+        const cudaLaunchConfig_t cfg = ctail_config(R, smem, nullptr, at);
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_mg_ctail, &cfg) != cudaSuccess || nclusters < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        H->ct_lt = lt;
+        H->ct_ls = ls;
+        H->ct_ranks = R;
+        H->ct_smem = smem;
+        return;
+    }
+}
+
+static int launch_ctail(pg_grid* g, const MgHierarchy& H, int nsmooth) {
+    CtArgs A{};
+    ctail_layout(H, H.ct_lt, H.ct_ls, H.ct_ranks, &A);
+    A.lt = H.ct_lt;
+    A.ls = H.ct_ls;
+    A.nl = H.nlev;
+    A.nsmooth = nsmooth;
+    A.ranks = H.ct_ranks;
+    A.e_out = H.lv[H.ct_lt].e;
+    A.f_in = H.lv[H.ct_lt].f;
+    cudaLaunchAttribute at[1];
+    const cudaLaunchConfig_t cfg = ctail_config(H.ct_ranks, H.ct_smem, g->stream, at);
+    cudaError_t err = cudaSuccess;
+    PG_LAUNCH(KK_MG_COARSE, g->stream, err = cudaLaunchKernelEx(&cfg, k_mg_ctail, A, g->ws.state));
+    if (err != cudaSuccess) return cuda_fail(err, "cluster tail launch");
+    return PG_OK;
+}
+
 // Launch one half-sweep over `color` at level l.
 template <bool L0, int MODE, bool RZ>
 static void smooth(pg_grid* g, const MgHierarchy& H, int l, float* e, const float* f, const float* ec, int color) {
@@ -1262,7 +1720,7 @@ static void smooth_lv(pg_grid* g, const MgHierarchy& H, int l, float* e, const f
 }
 
 // Enqueue z = V(r) on the grid's stream.
-static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, int nsmooth);
+static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, int nsmooth, int l0 = 0);
 
 // z = P V(P r): P removes the mean of every fluid component when there are
 // several (pg_pocket.cu); r is projected in place (the CG's recursive
@@ -1274,11 +1732,14 @@ static int vcycle_projected(pg_grid* g, const MgHierarchy& H, float* r, float* z
     return rc;
 }
 
-static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, int nsmooth) {
+// l0 = 1: only the coarse part, from level 1's f (already restricted) to
+// its correction e.
+static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, int nsmooth, int l0) {
     cudaStream_t s = g->stream;
     const int nl = H.nlev;
     auto E = [&](int l) -> float* { return l == 0 ? z : H.lv[l].e; };
     auto F = [&](int l) -> const float* { return l == 0 ? r : H.lv[l].f; };
+    if (l0 > 0 && nl == 1) return bad_arg("vcycle: no coarse levels");
     if (nl == 1) {
         // A grid too small to coarsen: symmetric Gauss-Seidel sweeps only.
         smooth_lv(g, H, 0, z, r, nullptr, 1, NB_FIRST);
@@ -1295,16 +1756,17 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
     }
     // levels [0, top) run as per-level kernels; [top, nl) in the tail kernel
     // (or, without a tail, the coarsest level alone in k_mg_coarse)
-    const bool tail = H.tail < nl;
-    const int top = tail ? H.tail : nl - 1;
+    const bool ctail = H.ct_lt > 0;
+    const bool tail = ctail || H.tail < nl;
+    const int top = ctail ? H.ct_lt : tail ? H.tail : nl - 1;
     // Fine level of 3D grids as fused pairs: 2 * nsmooth of them alternate
     // between the scratch and z (pair k writes pout[k & 1]), so the last one
     // lands in z; the pre-smoothed correction is pout[(nsmooth - 1) & 1].
     PairLaunch P;
-    const bool pairs = pair_plan(H, r, z, &P);
+    const bool pairs = l0 == 0 && pair_plan(H, r, z, &P);
     float* const pout[2] = {H.e0b, z};
     // down
-    for (int l = 0; l < top; ++l) {
+    for (int l = l0; l < top; ++l) {
         float* e = E(l);
         const float* f = F(l);
         if (l == 0 && pairs) {
@@ -1326,17 +1788,17 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
         if (l == 0 && pairs && restrict_tma(g, H, e, f, C.f)) {
         } else if (l == 0)
             PG_LAUNCH(KK_MG_RESTRICT, s,
-                      k_mg_restrict<true><<<blocks_for(g, nc), kMgThreads, 0, s>>>(v, e, f, C.f, (int)C.D.d,
+                      k_mg_restrict8<true><<<blocks_for(g, 8 * nc), kMgThreads, 0, s>>>(v, e, f, C.f, (int)C.D.d,
                                                                                  (int)C.D.h, (int)C.D.w,
                                                                                  g->ws.state));
         else
             PG_LAUNCH(KK_MG_RESTRICT_C, s,
-                      k_mg_restrict<false><<<blocks_for(g, nc), kMgThreads, 0, s>>>(v, e, f, C.f, (int)C.D.d,
+                      k_mg_restrict8<false><<<blocks_for(g, 8 * nc), kMgThreads, 0, s>>>(v, e, f, C.f, (int)C.D.d,
                                                                                   (int)C.D.h, (int)C.D.w,
                                                                                   g->ws.state));
     }
     if (tail) {
-        const int rc = launch_tail(g, H, nsmooth);
+        const int rc = ctail ? launch_ctail(g, H, nsmooth) : launch_tail(g, H, nsmooth);
         if (rc) return rc;
     } else {
         const LV v = view(H, nl - 1);
@@ -1344,7 +1806,7 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
                   k_mg_coarse<<<1, kCoarseThreads, 0, s>>>(v, H.lv[nl - 1].e, H.lv[nl - 1].f, g->ws.state));
     }
     // up
-    for (int l = top - 1; l >= 0; --l) {
+    for (int l = top - 1; l >= l0; --l) {
         float* e = E(l);
         const float* f = F(l);
         const float* ec = H.lv[l + 1].e;
@@ -1402,3 +1864,75 @@ template int solve_mgpcg<double>(pg_grid*, const pg_solver_params*, const CgConf
                                  pg_pcg_stats*);
 
 }  // namespace pg
+
+using namespace pg;
+
+// Device time of one V-cycle and of its coarse part (levels >= 1), each
+// captured once into a CUDA graph and replayed `reps` times between two
+// events on a private stream; r = 0 (the kernels' work does not depend on
+// the values).  Diagnostic: the coarse levels' kernels are too short to time
+// one by one without the timing itself dominating.
+extern "C" int pg_debug_mg_vcycle_ms(pg_grid* g, double dt, int nsmooth, int reps, double* full_ms,
+                                     double* coarse_ms) {
+    if (!g || !full_ms || !coarse_ms || reps < 1 || nsmooth < 1) return bad_arg("pg_debug_mg_vcycle_ms: bad argument");
+    MgHierarchy* H = nullptr;
+    int rc = ensure_mg(g, dt, &H);
+    if (rc) return rc;
+    if (H->nlev < 2) return bad_arg("pg_debug_mg_vcycle_ms: no coarse levels");
+    if ((rc = ensure_workspace(g))) return rc;
+    const size_t bytes = sizeof(float) * (size_t)g->dims.nc();
+    float *r = nullptr, *z = nullptr;
+    PG_CUDA(cudaMalloc(&r, bytes));
+    cudaError_t err = cudaMalloc(&z, bytes);
+    if (err != cudaSuccess) {
+        cudaFree(r);
+        return cuda_fail(err, "cudaMalloc(vcycle timing)");
+    }
+    cudaStream_t cs = nullptr, saved = g->stream;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    double out[2] = {0.0, 0.0};
+    err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreate(&ev[0]);
+    if (err == cudaSuccess) err = cudaEventCreate(&ev[1]);
+    if (err == cudaSuccess) err = cudaMemsetAsync(r, 0, bytes, cs);
+    if (err == cudaSuccess) err = cudaMemsetAsync(z, 0, bytes, cs);
+    if (err == cudaSuccess) err = cudaMemsetAsync(g->ws.state, 0, sizeof(CgState), cs);
+    for (int k = 0; k < 2 && err == cudaSuccess && rc == PG_OK; ++k) {
+        g->stream = cs;
+        prof_capture_begin();
+        err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+            rc = vcycle(g, *H, r, z, nsmooth, k);
+            const cudaError_t e2 = cudaStreamEndCapture(cs, &graph[k]);
+            if (err == cudaSuccess) err = e2;
+        }
+        prof_capture_end();
+        g->stream = saved;
+        if (err == cudaSuccess && rc == PG_OK) err = cudaGraphInstantiate(&exec[k], graph[k], 0);
+        for (int i = 0; i < 3 && err == cudaSuccess && rc == PG_OK; ++i) err = cudaGraphLaunch(exec[k], cs);
+        if (err == cudaSuccess && rc == PG_OK) err = cudaEventRecord(ev[0], cs);
+        for (int i = 0; i < reps && err == cudaSuccess && rc == PG_OK; ++i) err = cudaGraphLaunch(exec[k], cs);
+        if (err == cudaSuccess && rc == PG_OK) err = cudaEventRecord(ev[1], cs);
+        if (err == cudaSuccess && rc == PG_OK) err = cudaEventSynchronize(ev[1]);
+        float ms = 0.f;
+        if (err == cudaSuccess && rc == PG_OK) err = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        out[k] = (double)ms / reps;
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (exec[k]) cudaGraphExecDestroy(exec[k]);
+        if (graph[k]) cudaGraphDestroy(graph[k]);
+    }
+    if (cs) cudaStreamSynchronize(cs);
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+    if (cs) cudaStreamDestroy(cs);
+    cudaFree(r);
+    cudaFree(z);
+    if (rc) return rc;
+    if (err != cudaSuccess) return cuda_fail(err, "pg_debug_mg_vcycle_ms");
+    *full_ms = out[0];
+    *coarse_ms = out[1];
+    return PG_OK;
+}

@@ -228,7 +228,7 @@ def test_mg_with_isolated_pockets(pg, oracle, dims):
     assert np.abs(oracle.divergence_rhs(v, dims, fs)).max() <= 1e-5 * st["b_max"] + 1e-6 * np.abs(v).max()
 
 
-def _pair_launches(lib, fn):
+def _launches(lib, fn, kind):
     import ctypes as C
 
     names = [lib.pg_profile_kind_name(k).decode() for k in range(lib.pg_profile_num_kinds())]
@@ -239,8 +239,12 @@ def _pair_launches(lib, fn):
     finally:
         lib.pg_profile_enable(0)
     t, n = C.c_double(), C.c_int64()
-    lib.pg_profile_read(names.index("mg_pair"), C.byref(t), C.byref(n))
+    lib.pg_profile_read(names.index(kind), C.byref(t), C.byref(n))
     return out, n.value
+
+
+def _pair_launches(lib, fn):
+    return _launches(lib, fn, "mg_pair")
 
 
 @pytest.mark.parametrize("dims", [(20, 24, 80), (37, 19, 48), (64, 64, 64)])
@@ -330,3 +334,49 @@ def test_tma_restriction_equals_plain_kernel(pg, oracle, dims, monkeypatch):
     (s1, x1), (s0, x0) = res["1"], res["0"]
     assert s1["iterations"] == s0["iterations"]
     assert np.array_equal(x1, x0)
+
+
+@pytest.mark.parametrize("dims", [(64, 64, 64), (96, 64, 80), (48, 40, 64), (20, 24, 80), (128, 128, 128)])
+@pytest.mark.parametrize("nsmooth", [1, 2])
+def test_cluster_tail_equals_per_level_kernels(pg, oracle, dims, nsmooth, monkeypatch):
+    """The cluster tail (levels of at most 32768 cells in one thread-block
+    cluster: z slabs per rank in distributed shared memory, the smallest
+    levels in rank 0) computes every cell with the per-level kernels' and the
+    single-block tail's formulas: the solves are bit-identical with
+    PG_MG_CTAIL=0, on shapes whose slabs leave ranks empty, with an
+    obstacle, for 1 and 2 sweeps."""
+    lib = pg.load()
+    r = rng(seed_of(dims, nsmooth, "ctail"))
+    idx = np.indices(dims).astype(np.float64)
+    ctr = np.array([(n - 1) / 2 for n in dims]).reshape((-1, 1, 1, 1))
+    cs = (((idx - ctr) ** 2).sum(0) < (min(dims) / 4.0) ** 2).astype(np.uint8)
+    nf = oracle.num_faces(dims)
+    vel = oracle.walls(r.standard_normal(nf).astype(np.float32), dims)
+    res = {}
+    for on in ("1", "0"):
+        monkeypatch.setenv("PG_MG_CTAIL", on)
+        g = make_grid(pg, dims)  # a new grid builds its hierarchy under the switch
+        g.set_solid_cells(cs)
+        b = g.new_simplex_2()
+        g.divergence_rhs(b, faces(pg, g, vel))
+        x = g.new_simplex_2()
+        cfg = pg.SolverConfig(precond=2, rel_stop=True, rel_tol=1e-6, max_iter=2000, refine=4, mg_smooth=nsmooth)
+        st, n_coarse = _launches(lib, lambda: pg.solve_pressure(g, x, b, 0.5, cfg), "mg_smooth_coarse")
+        assert st["status"] == 0 and st["true_residual_max"] <= 1e-6 * st["b_max"], (on, st)
+        res[on] = (st, host(x), n_coarse)
+    (s1, x1, n1), (s0, x0, n0) = res["1"], res["0"]
+    assert n1 < n0, (n1, n0)  # the cluster took over the half-sweeps of its top level
+    assert s1["iterations"] == s0["iterations"]
+    assert np.array_equal(x1, x0)
+
+
+def test_vcycle_graph_timing(pg):
+    """pg_debug_mg_vcycle_ms replays one V-cycle and its coarse part as CUDA
+    graphs: both times are positive and the coarse part is the smaller."""
+    import ctypes as C
+
+    lib = pg.load()
+    g = make_grid(pg, (64, 64, 64))
+    full, coarse = C.c_double(), C.c_double()
+    assert lib.pg_debug_mg_vcycle_ms(g.handle, C.c_double(0.5), 2, 5, C.byref(full), C.byref(coarse)) == 0
+    assert 0.0 < coarse.value < full.value, (full.value, coarse.value)
