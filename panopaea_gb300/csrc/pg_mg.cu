@@ -25,7 +25,9 @@
 // on the fly there.  The last fine-level half-sweep writes z and reduces
 // z.r into the CG state.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
+#include <vector>
 
 #include "pg_solve.cuh"
 #include "pg_tma.cuh"
@@ -36,6 +38,7 @@ constexpr int kMgThreads = 256;
 constexpr int kCoarseMax = 2048;
 constexpr int kCoarseThreads = 512;
 constexpr int kMaxLevels = 16;
+constexpr int kCinvCells = 64;  // coarsest levels up to this size are solved by a dense pseudo-inverse
 constexpr int kTailCells = 4096;  // levels at most this large run in the single-block tail
 
 struct MgLevel {
@@ -59,6 +62,7 @@ struct MgHierarchy {
     uint64_t id = 0;  // unique per build (CUDA-graph cache key)
     Pockets pockets;  // fluid components (empty when the fluid is connected)
     int tail = 0;     // first level handled by the single-block tail kernel (nlev: none)
+    float* cinv = nullptr;  // coarsest level of at most kCinvCells cells: its pseudo-inverse (row-major)
     int ct_lt = 0;    // cluster tail (3D): first level (0: not used), first rank-0 level, ranks
     int ct_ls = 0;
     int ct_ranks = 0;
@@ -730,6 +734,7 @@ struct TailArgs {
     int lt, nl, nsmooth;
     float* e_out;       // global e of level lt
     const float* f_in;  // global f of level lt
+    const float* cinv;  // the coarsest level's pseudo-inverse, or null
     TailLevel L[kMaxLevels];
 };
 
@@ -835,8 +840,24 @@ __device__ __forceinline__ void tail_restrict(const LV& v, const float* e, const
 // Coarsest level: symmetric red-black Gauss-Seidel from e = 0 (`pairs`
 // (red, black) sweeps, then `pairs` (black, red)); a level of at most 256
 // cells is swept by warp 0 alone, with warp barriers.
-__device__ __forceinline__ void tail_coarsest(const LV& cv, float* e, const float* f) {
+__device__ __forceinline__ void tail_coarsest(const LV& cv, float* e, const float* f, const float* cinv) {
     const int n = cv.d * cv.h * cv.w;
+    if (cinv) {
+        // e = pinv(A) f: 16 lanes per row, each summing every 16th column,
+        // then a fixed butterfly over the 16 (deterministic)
+        const int nr = (n * 16 + 31) & ~31;  // whole warps
+        for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+            const int i = t >> 4, j = t & 15;
+            float acc = 0.f;
+            if (i < n)
+                for (int k = j; k < n; k += 16) acc += cinv[i * n + k] * f[k];
+#pragma unroll
+            for (int m = 8; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+            if (j == 0 && i < n) e[i] = acc;
+        }
+        __syncthreads();
+        return;
+    }
     const int pairs = coarse_pairs(cv.d, cv.h, cv.w);
     if (n <= 256) {
         if (threadIdx.x < 32) {
@@ -920,7 +941,7 @@ __device__ __forceinline__ void tail_body(const TailArgs& A, float* tsm) {
         }
         tail_restrict(v, e, f, F(l + 1), c.d, c.h, c.w);
     }
-    tail_coarsest(lv(nl - 1), E(nl - 1), F(nl - 1));
+    tail_coarsest(lv(nl - 1), E(nl - 1), F(nl - 1), A.cinv);
     // up
     for (int l = nl - 2; l >= A.lt; --l) {
         const TailLevel& c = A.L[l + 1];
@@ -978,6 +999,7 @@ struct CtArgs {
     int lt, ls, nl, nsmooth, ranks;
     float* e_out;       // global e of level lt
     const float* f_in;  // global f of level lt
+    const float* cinv;  // the coarsest level's pseudo-inverse, or null
     CtLevel L[kMaxLevels];
 };
 
@@ -1187,7 +1209,7 @@ __global__ void __launch_bounds__(kCtThreads) k_mg_ctail(CtArgs A, CgState* st) 
             }
             tail_restrict(v, e, f, F(l + 1), c.d, c.h, c.w);
         }
-        tail_coarsest(lv(nl - 1), E(nl - 1), F(nl - 1));
+        tail_coarsest(lv(nl - 1), E(nl - 1), F(nl - 1), A.cinv);
         for (int l = nl - 2; l >= ls; --l) {
             const CtLevel& c = A.L[l + 1];
             const LV v = lv(l);
@@ -1287,6 +1309,7 @@ void release_mg(Extras* ex) {
         release_pockets(&ex->mg->pockets);
         cudaFree(ex->mg->mem);
         cudaFree(ex->mg->e0b);
+        cudaFree(ex->mg->cinv);
         delete ex->mg;
         ex->mg = nullptr;
     }
@@ -1296,6 +1319,97 @@ static int blocks_for(const pg_grid* g, i64 n) { return grid_blocks(g, n, kMgThr
 
 static int pair_setup(pg_grid* g, MgHierarchy* H);
 static void ctail_setup(MgHierarchy* H);
+
+// Moore-Penrose pseudo-inverse of the symmetric n x n matrix a (row-major,
+// overwritten) by cyclic Jacobi rotations in double; eigenvalues below
+// 1e-10 of the largest count as zero (the constant mode of every closed
+// fluid component, and cells without open faces).
+static void sym_pinv(int n, std::vector<double>& a) {
+    std::vector<double> v((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) v[(size_t)i * n + i] = 1.0;
+    auto A = [&](int i, int j) -> double& { return a[(size_t)i * n + j]; };
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) (i == j ? tot : off) += A(i, j) * A(i, j);
+        if (off <= 1e-30 * (tot + off)) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A(p, q);
+                if (apq == 0.0) continue;
+                const double theta = (A(q, q) - A(p, p)) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < n; ++k) {  // columns p, q
+                    const double akp = A(k, p), akq = A(k, q);
+                    A(k, p) = c * akp - sn * akq;
+                    A(k, q) = sn * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {  // rows p, q
+                    const double apk = A(p, k), aqk = A(q, k);
+                    A(p, k) = c * apk - sn * aqk;
+                    A(q, k) = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = v[(size_t)k * n + p], vkq = v[(size_t)k * n + q];
+                    v[(size_t)k * n + p] = c * vkp - sn * vkq;
+                    v[(size_t)k * n + q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    double lmax = 0.0;
+    for (int i = 0; i < n; ++i) lmax = std::max(lmax, std::fabs(A(i, i)));
+    std::vector<double> lam(n);
+    for (int i = 0; i < n; ++i) lam[i] = A(i, i);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            double sum = 0.0;
+            for (int k = 0; k < n; ++k)
+                if (lam[k] > 1e-10 * lmax) sum += v[(size_t)i * n + k] * v[(size_t)j * n + k] / lam[k];
+            A(i, j) = sum;
+        }
+}
+
+// The coarsest level's operator (its face weights; the diagonal is their
+// sum, as 1/diag is) and its pseudo-inverse on the device, when the level
+// has at most kCinvCells cells (PG_MG_CINV=0 keeps the Gauss-Seidel sweeps;
+// a diagnostic switch read per build).
+static int coarsest_pinv(pg_grid* g, MgHierarchy* H) {
+    const int nl = H->nlev;
+    const char* env = getenv("PG_MG_CINV");
+    if (nl < 2 || (env && env[0] == '0')) return PG_OK;
+    const MgLevel& L = H->lv[nl - 1];
+    const int n = (int)L.D.nc(), d = (int)L.D.d, h = (int)L.D.h, w = (int)L.D.w;
+    if (n > kCinvCells) return PG_OK;
+    std::vector<float> wx(n), wy(n), wz(n, 0.f);
+    PG_CUDA(cudaMemcpyAsync(wx.data(), L.wx, sizeof(float) * n, cudaMemcpyDeviceToHost, g->stream));
+    PG_CUDA(cudaMemcpyAsync(wy.data(), L.wy, sizeof(float) * n, cudaMemcpyDeviceToHost, g->stream));
+    if (L.D.nd == 3) PG_CUDA(cudaMemcpyAsync(wz.data(), L.wz, sizeof(float) * n, cudaMemcpyDeviceToHost, g->stream));
+    PG_CUDA(cudaStreamSynchronize(g->stream));
+    std::vector<double> a((size_t)n * n, 0.0);
+    auto link = [&](int c, int k, float wt) {  // face between cells c and k
+        if (wt == 0.f) return;
+        a[(size_t)c * n + c] += wt;
+        a[(size_t)k * n + k] += wt;
+        a[(size_t)c * n + k] -= wt;
+        a[(size_t)k * n + c] -= wt;
+    };
+    for (int z = 0; z < d; ++z)
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < w; ++x) {
+                const int c = (z * h + y) * w + x;
+                if (x > 0) link(c, c - 1, wx[c]);
+                if (y > 0) link(c, c - w, wy[c]);
+                if (z > 0) link(c, c - h * w, wz[c]);
+            }
+    sym_pinv(n, a);
+    std::vector<float> m((size_t)n * n);
+    for (size_t i = 0; i < m.size(); ++i) m[i] = (float)a[i];
+    PG_CUDA(cudaMalloc(&H->cinv, sizeof(float) * m.size()));
+    PG_CUDA(cudaMemcpyAsync(H->cinv, m.data(), sizeof(float) * m.size(), cudaMemcpyHostToDevice, g->stream));
+    PG_CUDA(cudaStreamSynchronize(g->stream));
+    return PG_OK;
+}
 
 // (Re)build the hierarchy for the grid's current mask and dt.
 static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
@@ -1406,6 +1520,7 @@ static int ensure_mg(pg_grid* g, double dt, MgHierarchy** out) {
         PG_LAUNCH(KK_MG_SETUP, s, k_mg_invd<<<blocks_for(g, nc), kMgThreads, 0, s>>>(cv, C.invd));
     }
     PG_CHECK_LAUNCH();
+    if (const int crc = coarsest_pinv(g, H)) return crc;
     *out = H;
     return PG_OK;
 }
@@ -1560,6 +1675,7 @@ static TailArgs tail_args(const MgHierarchy& H, int nsmooth) {
     A.nsmooth = nsmooth;
     A.e_out = H.lv[H.tail].e;
     A.f_in = H.lv[H.tail].f;
+    A.cinv = H.cinv;
     for (int l = H.tail; l < H.nlev; ++l) {
         const MgLevel& L = H.lv[l];
         A.L[l] = TailLevel{L.D.nd, (int)L.D.d, (int)L.D.h, (int)L.D.w, L.wx, L.wy, L.wz, L.invd};
@@ -1679,6 +1795,7 @@ static int launch_ctail(pg_grid* g, const MgHierarchy& H, int nsmooth) {
     A.ranks = H.ct_ranks;
     A.e_out = H.lv[H.ct_lt].e;
     A.f_in = H.lv[H.ct_lt].f;
+    A.cinv = H.cinv;
     cudaLaunchAttribute at[1];
     const cudaLaunchConfig_t cfg = ctail_config(H.ct_ranks, H.ct_smem, g->stream, at);
     cudaError_t err = cudaSuccess;
