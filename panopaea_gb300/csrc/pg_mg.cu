@@ -173,7 +173,47 @@ __global__ void __launch_bounds__(kMgThreads)
         const int row = i / half, k2 = i - row * half;
         const int z = row / v.h, y = row - z * v.h;
         const int x = 2 * k2 + ((y + z + color) & 1);
-        if (x < v.w) {
+        if (!L0 && x < v.w) {
+            // Coarse levels (weights in memory): every value the cell may
+            // need is loaded before any is used -- a missing neighbour's
+            // offset is clamped to the cell itself and its value ignored --
+            // so the cell waits for one round of loads; the arithmetic is
+            // the same as below.
+            const int c = row * v.w + x;
+            const bool d3 = v.nd == 3;
+            const bool hx = x + 1 < v.w, hy = y + 1 < v.h, hz = d3 && z + 1 < v.d;
+            const int ox0 = x > 0 ? -1 : 0, ox1 = hx ? 1 : 0, oy0 = y > 0 ? -v.w : 0, oy1 = hy ? v.w : 0;
+            const int oz0 = d3 && z > 0 ? -hw : 0, oz1 = hz ? hw : 0;
+            const float wxl = v.wx[c], wxh_ = v.wx[c + ox1], wyl = v.wy[c], wyh_ = v.wy[c + oy1];
+            const float wzl = d3 ? v.wz[c] : 0.f, wzh_ = d3 ? v.wz[c + oz1] : 0.f;
+            const float inv = v.invd[c];
+            float s = f[c];
+            if (MODE == NB_SELF) {
+                e[c] = s * inv;
+                continue;
+            }
+            const float n0 = nbval<L0, MODE>(v, e, f, ec, cw, ch, c + ox0, z, y, x + (x > 0 ? -1 : 0));
+            const float n1 = nbval<L0, MODE>(v, e, f, ec, cw, ch, c + ox1, z, y, x + ox1);
+            const float n2 = nbval<L0, MODE>(v, e, f, ec, cw, ch, c + oy0, z, y + (y > 0 ? -1 : 0), x);
+            const float n3 = nbval<L0, MODE>(v, e, f, ec, cw, ch, c + oy1, z, y + (hy ? 1 : 0), x);
+            const float n4 = nbval<L0, MODE>(v, e, f, ec, cw, ch, c + oz0, z + (oz0 ? -1 : 0), y, x);
+            const float n5 = nbval<L0, MODE>(v, e, f, ec, cw, ch, c + oz1, z + (hz ? 1 : 0), y, x);
+            const float wxh = hx ? wxh_ : 0.f, wyh = hy ? wyh_ : 0.f, wzh = hz ? wzh_ : 0.f;
+            if (wxl != 0.f) s += wxl * n0;
+            if (wxh != 0.f) s += wxh * n1;
+            if (wyl != 0.f) s += wyl * n2;
+            if (wyh != 0.f) s += wyh * n3;
+            if (d3) {
+                if (wzl != 0.f) s += wzl * n4;
+                if (wzh != 0.f) s += wzh * n5;
+            }
+            const float en = s * inv;
+            e[c] = en;
+            if (RZ) {
+                acc.add(en * f[c]);
+                zs.add(en);
+            }
+        } else if (x < v.w) {
             const int c = row * v.w + x;
             const Cell<L0> cl(v, c, z, y, x);
             float s = f[c];
@@ -649,15 +689,22 @@ __global__ void __launch_bounds__(kMgThreads)
             if (z < z1 && y < v.h && x < v.w) {
                 const int c = (z * v.h + y) * v.w + x;
                 const Cell<L0> cl(v, c, z, y, x);
-                const float ecv = e[c];
+                // every neighbour value loaded at once (offsets of missing
+                // neighbours clamped to the cell, their values ignored)
+                const bool d3 = v.nd == 3;
+                const int ox0 = x > 0 ? -1 : 0, ox1 = x + 1 < v.w ? 1 : 0;
+                const int oy0 = y > 0 ? -v.w : 0, oy1 = y + 1 < v.h ? v.w : 0;
+                const int oz0 = d3 && z > 0 ? -hw : 0, oz1 = d3 && z + 1 < v.d ? hw : 0;
+                const float ecv = e[c], e0 = e[c + ox0], e1 = e[c + ox1], e2 = e[c + oy0], e3 = e[c + oy1],
+                            e4 = e[c + oz0], e5 = e[c + oz1];
                 float a = 0.f;
-                if (cl.wxl != 0.f) a += cl.wxl * (ecv - e[c - 1]);
-                if (cl.wxh != 0.f) a += cl.wxh * (ecv - e[c + 1]);
-                if (cl.wyl != 0.f) a += cl.wyl * (ecv - e[c - v.w]);
-                if (cl.wyh != 0.f) a += cl.wyh * (ecv - e[c + v.w]);
-                if (v.nd == 3) {
-                    if (cl.wzl != 0.f) a += cl.wzl * (ecv - e[c - hw]);
-                    if (cl.wzh != 0.f) a += cl.wzh * (ecv - e[c + hw]);
+                if (cl.wxl != 0.f) a += cl.wxl * (ecv - e0);
+                if (cl.wxh != 0.f) a += cl.wxh * (ecv - e1);
+                if (cl.wyl != 0.f) a += cl.wyl * (ecv - e2);
+                if (cl.wyh != 0.f) a += cl.wyh * (ecv - e3);
+                if (d3) {
+                    if (cl.wzl != 0.f) a += cl.wzl * (ecv - e4);
+                    if (cl.wzh != 0.f) a += cl.wzh * (ecv - e5);
                 }
                 term = f[c] - a;
                 has = true;
