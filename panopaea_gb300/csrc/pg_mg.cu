@@ -1832,10 +1832,7 @@ static void ctail_setup(MgHierarchy* H) {
             break;
         }
     if (ls <= lt || ls > nl - 1) return;
-    const char* renv = getenv("PG_MG_CTAIL_RANKS");
-    const int only = renv ? atoi(renv) : 0;
     for (int R : {16, 8}) {
-        if (only && R != only) continue;
         CtArgs A{};
         const size_t smem = ctail_layout(*H, lt, ls, R, &A);
         if (smem == 0) continue;
