@@ -601,6 +601,23 @@ static bool cg_tma_enabled() {
     return !(env && env[0] == '0');
 }
 
+// The update of the identity / Jacobi CG: the float4 kernel where every
+// vector and the flags are 16-byte aligned and the cell count is a multiple
+// of 4, else the scalar kernel.  Every entry point of that CG launches its
+// update here, so they compute the same iterates on the same buffers.
+template <class T, int PM>
+static void update_launch(cudaStream_t s, int nb, T* x, T* r, const T* p0, const T* p1, const T* ap,
+                          const uint8_t* flags, i64 n, T dt, CgState* st, double* partials) {
+    const bool vec4 = sizeof(T) == 4 && n % 4 == 0 && aligned16(x) && aligned16(r) && aligned16(p0) &&
+                      aligned16(p1) && aligned16(ap) && aligned16(flags);
+    if (vec4)
+        k_cg_update4r<PM><<<nb, kCgThreads, 0, s>>>((float4*)x, (float4*)r, (const float4*)p0, (const float4*)p1,
+                                                    (const float4*)ap, (const uchar4*)flags, n / 4, (float)dt, st,
+                                                    partials);
+    else
+        k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(x, r, p0, p1, ap, flags, n, dt, st, partials);
+}
+
 template <class T, int PM>
 static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook* hook) {
     const Dims& D = g->dims;
@@ -622,12 +639,10 @@ static void launch_iter(pg_grid* g, const CgBuffers<T>& buf, T dt, int nb, ZHook
                                                                 (const float4*)buf.p[0], (const float4*)buf.p[1],
                                                                 (const float4*)buf.ap, n / 4, g->ws.state,
                                                                 g->ws.partials, nullptr));
-    else if (PM != PM_ZBUF && vec4)
+    else if (PM != PM_ZBUF)
         PG_LAUNCH(KK_CG_UPDATE, s,
-                  k_cg_update4r<PM><<<nb, kCgThreads, 0, s>>>((float4*)buf.x, (float4*)buf.r,
-                                                              (const float4*)buf.p[0], (const float4*)buf.p[1],
-                                                              (const float4*)buf.ap, (const uchar4*)g->flags, n / 4,
-                                                              (float)dt, g->ws.state, g->ws.partials));
+                  update_launch<T, PM>(s, nb, buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, n, dt, g->ws.state,
+                                       g->ws.partials));
     else
         PG_LAUNCH(KK_CG_UPDATE, s,
                   k_cg_update<T, PM><<<nb, kCgThreads, 0, s>>>(buf.x, buf.r, buf.p[0], buf.p[1], buf.ap, g->flags, n,
@@ -969,9 +984,8 @@ static int run(const Dims& D, const uint8_t* flags, float* x, const float* b, i6
         const i64 todo = std::min<i64>(chunk, max_iter - done_launch);
         for (i64 k = 0; k < todo; ++k) {
             spmv_launch<float, PM>(s, sms, residual, nullptr, p[0], p[1], auxiliary, flags, D, fdt, st, partials, nb,
-                                   false);
-            k_cg_update<float, PM><<<nb, kCgThreads, 0, s>>>(x, residual, p[0], p[1], auxiliary, flags, n, fdt, st,
-                                                             partials);
+                                   cg_tma_enabled());
+            update_launch<float, PM>(s, nb, x, residual, p[0], p[1], auxiliary, flags, n, fdt, st, partials);
         }
         PG_CHECK_LAUNCH();
         launches += 2 * todo;
