@@ -18,6 +18,7 @@ template <class T> struct CgBuffers {
     T* p[2];
     T* z = nullptr;   // PM_ZBUF only
     T* xl = nullptr;  // PM_ZBUF, float, n % 4 == 0: x held as the double-float pair (x, xl)
+                      // and started from 0 (see run_cg_pm)
 };
 
 struct CgConfig {
@@ -76,6 +77,9 @@ struct ZHook {
     // The CG's A p vector (read by flexible-CG hooks for beta), given before
     // the first apply().
     virtual void bind(const void* ap) { (void)ap; }
+    // Whether apply() writes r (an in-place projection): the CG then cannot
+    // hand it the right-hand side itself for the first application.
+    virtual bool writes_input() const { return true; }
     virtual ~ZHook() {}
 };
 

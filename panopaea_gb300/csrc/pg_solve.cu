@@ -543,7 +543,9 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
             break;
         }
         if (dfx) {
-            // x already holds the round's iterate
+            // x holds the round's iterate -- written by its first update, so
+            // a round that made none leaves it to be zeroed here
+            if (s.iterations == 0) PG_CUDA(cudaMemsetAsync(x64, 0, sizeof(double) * n, g->stream));
         } else if (from_b) {  // x was 0: x = d
             if (native)
                 PG_LAUNCH(KK_REFINE_UPDATE, g->stream, k_x64_set<<<nb, kThreads, 0, g->stream>>>((double*)x64, (const float*)d, n));
