@@ -212,3 +212,49 @@ def test_batch_mg_long_run_converges(pg):
         st = B.step(cfg, v, rho, p, source_field=src)
         bad = [(i, s["iterations"], s["status"]) for i, s in enumerate(st) if s["status"] != 0 or s["iterations"] > 12]
         assert not bad, (k, bad[:5])
+
+
+@pytest.mark.parametrize("precond", [1, 2])
+def test_batch_steps_against_fp64_oracle(pg, oracle, precond):
+    """Each batched step against the oracle's all-FP64 step (FP64 fields,
+    FP64 Jacobi-PCG to relative 1e-10) taken from the same input state (the
+    batch's state after the previous step), on 6 grids of 64..192 cells per
+    side with solid circles and boundary sources: the batch solves in FP32
+    to relative 1e-6 without refinement, so its projected velocity may differ
+    by the FP32 solve's error -- within 2e-4 of max |u| per grid (measured
+    at most 6.5e-5) -- and the density, advected in FP32 by the previous
+    velocity, by the FP32 rounding of back-traced positions of up to ~200
+    cells (~1e-5 cells) times the sources' gradient -- within 2e-5 of max rho
+    (measured at most 3.2e-6)."""
+    from panopaea_gb300 import workloads as W
+
+    dims, masks, srcs = W.batch_grids(6, seed=21, sides=tuple(range(64, 193, 32)))
+    B = pg.Batch2d(dims)
+    B.set_solid_cells(masks)
+    v, rho, p = B.new_faces(), B.new_cells(), B.new_cells()
+    src = torch.from_numpy(B.pack_cells(srcs)).cuda()
+    cfg = pg.StepConfig(dt=0.5, buoyancy=1.0, source_enabled=False, walls_after_advect=True,
+                        zero_solid_after_project=True,
+                        solver=pg.SolverConfig(precond=precond, rel_stop=True, rel_tol=1e-6, max_iter=5000))
+    fss = [oracle.cell_mask_to_faces(m) for m in masks]
+    worst_v = worst_r = 0.0
+    for step in range(3):
+        torch.cuda.synchronize()
+        ins = [(B.faces_of(v, i).cpu().numpy().astype(np.float64), B.cells_of(rho, i).cpu().numpy().astype(np.float64),
+                B.cells_of(p, i).cpu().numpy().astype(np.float64)) for i in range(len(dims))]
+        st = B.step(cfg, v, rho, p, source_field=src)
+        torch.cuda.synchronize()
+        for i, d in enumerate(dims):
+            vel, r64, p64 = ins[i]
+            prm = oracle.step_params(dt=0.5, buoyancy=1.0, walls_after_advect=True, zero_solid_after_project=True,
+                                     precond=1, rel_stop=True, rel_tol=1e-10, max_iter=100000,
+                                     source_field=srcs[i].astype(np.float64))
+            so = oracle.step(vel, r64, p64, d, prm, fss[i])
+            assert so.converged and st[i]["status"] == 0, (step, i)
+            gv = B.faces_of(v, i).cpu().numpy().astype(np.float64)
+            gr = B.cells_of(rho, i).cpu().numpy().astype(np.float64)
+            ev = np.abs(gv - vel).max() / max(np.abs(vel).max(), 1e-30)
+            er = np.abs(gr - r64).max() / max(np.abs(r64).max(), 1e-30)
+            worst_v, worst_r = max(worst_v, ev), max(worst_r, er)
+            assert ev <= 2e-4 and er <= 2e-5, (step, i, d, ev, er)
+    print("worst velocity %.2e density %.2e" % (worst_v, worst_r))
