@@ -167,7 +167,7 @@ __device__ __forceinline__ float nbval(const LV& v, const float* __restrict__ e,
 template <bool L0, int MODE, bool RZ>
 __global__ void __launch_bounds__(kMgThreads)
     k_mg_smooth(LV v, float* __restrict__ e, const float* __restrict__ f, const float* __restrict__ ec, int cw, int ch,
-                int color, CgState* st, double* partials) {
+                int color, CgState* st, double* partials, FastDiv fhalf, FastDiv fh) {
     if (st->done) return;
     __shared__ double sm[32];
     const int hw = v.h * v.w;
@@ -176,8 +176,12 @@ __global__ void __launch_bounds__(kMgThreads)
     const int total = nrow * half;
     Acc<float> acc, zs;  // z.r and sum(z) (RZ)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const int row = i / half, k2 = i - row * half;
-        const int z = row / v.h, y = row - z * v.h;
+        // the flat index split by invariant-divisor multiplication (the
+        // coarse half-sweeps are issue-bound: two integer divisions were
+        // a quarter of a cell's instructions)
+        int k2, y;
+        const int row = split(i, half, fhalf, k2);
+        const int z = split(row, v.h, fh, y);
         const int x = 2 * k2 + ((y + z + color) & 1);
         if (!L0 && x < v.w) {
             // Coarse levels (weights in memory): every value the cell may
@@ -248,8 +252,9 @@ __global__ void __launch_bounds__(kMgThreads)
     // half-sweep -- reduce both colours: the black part is added by the
     // companion pass below (same kernel, other colour read-only).
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const int row = i / half, k2 = i - row * half;
-        const int z = row / v.h, y = row - z * v.h;
+        int k2, y;
+        const int row = split(i, half, fhalf, k2);
+        const int z = split(row, v.h, fh, y);
         const int x = 2 * k2 + ((y + z + color + 1) & 1);
         if (x < v.w) {
             const int c = row * v.w + x;
@@ -1904,8 +1909,9 @@ static void smooth(pg_grid* g, const MgHierarchy& H, int l, float* e, const floa
     }
     cudaStream_t s = g->stream;
     PG_LAUNCH(l == 0 ? KK_MG_SMOOTH : KK_MG_SMOOTH_C, s,
-              k_mg_smooth<L0, MODE, RZ><<<blocks_for(g, n), kMgThreads, 0, s>>>(v, e, f, ec, cw, ch, color,
-                                                                                g->ws.state, g->ws.partials));
+              k_mg_smooth<L0, MODE, RZ><<<blocks_for(g, n), kMgThreads, 0, s>>>(
+                  v, e, f, ec, cw, ch, color, g->ws.state, g->ws.partials, fast_div((unsigned)((v.w + 1) >> 1)),
+                  fast_div((unsigned)v.h)));
 }
 
 template <bool L0>
