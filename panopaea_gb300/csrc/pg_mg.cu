@@ -714,12 +714,13 @@ __device__ __forceinline__ float child_residual(const LV& v, const float* __rest
 template <bool L0>
 __global__ void __launch_bounds__(kMgThreads)
     k_mg_restrict(LV v, const float* __restrict__ e, const float* __restrict__ f, float* __restrict__ fc, int cd,
-                  int ch, int cw, CgState* st) {
+                  int ch, int cw, CgState* st, FastDiv fcw, FastDiv fch) {
     if (st->done) return;
     const int nc = cd * ch * cw;
     for (int C = blockIdx.x * blockDim.x + threadIdx.x; C < nc; C += gridDim.x * blockDim.x) {
-        const int CZY = C / cw, X = C - CZY * cw;
-        const int Z = CZY / ch, Y = CZY - Z * ch;
+        int X, Y;
+        const int CZY = split(C, cw, fcw, X);
+        const int Z = split(CZY, ch, fch, Y);
         float sum = 0.f;
         const int z1 = v.nd == 3 ? min(2 * Z + 2, v.d) : 1;
         const int y1 = min(2 * Y + 2, v.h), x1 = min(2 * X + 2, v.w);
@@ -736,7 +737,7 @@ __global__ void __launch_bounds__(kMgThreads)
 template <bool L0>
 __global__ void __launch_bounds__(kMgThreads)
     k_mg_restrict8(LV v, const float* __restrict__ e, const float* __restrict__ f, float* __restrict__ fc, int cd,
-                   int ch, int cw, CgState* st) {
+                   int ch, int cw, CgState* st, FastDiv fcw, FastDiv fch) {
     if (st->done) return;
     const int nc = cd * ch * cw;
     const unsigned lane = threadIdx.x & 31, grp = lane & ~7u;
@@ -747,8 +748,9 @@ __global__ void __launch_bounds__(kMgThreads)
         float term = 0.f;
         bool has = false;
         if (C < nc) {
-            const int CZY = C / cw, X = C - CZY * cw;
-            const int Z = CZY / ch, Y = CZY - Z * ch;
+            int X, Y;
+            const int CZY = split(C, cw, fcw, X);
+            const int Z = split(CZY, ch, fch, Y);
             const int z = (v.nd == 3 ? 2 * Z : 0) + (j >> 2), y = 2 * Y + ((j >> 1) & 1), x = 2 * X + (j & 1);
             const int z1 = v.nd == 3 ? min(2 * Z + 2, v.d) : 1;
             if (z < z1 && y < v.h && x < v.w) {
@@ -1082,6 +1084,7 @@ struct CtLevel {
     int ppc;  // planes per rank (d: the level lives in rank 0)
     int off;  // offset (floats) of the level's block [wx | wy | wz | invd | e | f] in shared memory
     int P;    // floats per array of the block: ppc * h * w
+    FastDiv fhalf, fh, fw, fhw, fppc;  // invariant divisors (w + 1) / 2, h, w, h * w, ppc
     const float* wx;
     const float* wy;
     const float* wz;
@@ -1114,8 +1117,9 @@ __device__ __forceinline__ void ct_sync() {
 
 // Array 0 (wx) of level L at plane z, on the rank that owns it.
 __device__ __forceinline__ float* ct_plane(float* const* peer, const CtLevel& L, int z) {
-    const int r = z / L.ppc;
-    return peer[r] + L.off + (z - r * L.ppc) * L.h * L.w;
+    int zl;
+    const int r = split(z, L.ppc, L.fppc, zl);
+    return peer[r] + L.off + zl * L.h * L.w;
 }
 
 // Neighbour value of the smoother at the cell whose array-0 entry is q
@@ -1143,8 +1147,9 @@ __device__ void ct_smooth(float* const* peer, const CtLevel& L, const CtLevel* L
     const int half = (w + 1) >> 1, total = nz * h * half;
     float* B = peer[rank] + L.off;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
-        const int row = i / half, k2 = i - row * half;
-        const int zl = row / h, y = row - zl * h, z = z0 + zl;
+        int k2, y;
+        const int row = split(i, half, L.fhalf, k2);
+        const int zl = split(row, h, L.fh, y), z = z0 + zl;
         const int x = 2 * k2 + ((y + z + color) & 1);
         if (x >= w) continue;
         const int c = row * w + x;
@@ -1191,8 +1196,9 @@ __device__ void ct_restrict(float* const* peer, const CtLevel& L, const CtLevel&
     const int n8 = (total * 8 + 31) & ~31;  // whole warps: every lane runs the same trips
     for (int t = threadIdx.x; t < n8; t += blockDim.x) {
         const int i = t >> 3, j = t & 7;
-        const int Z = Z0 + i / chw, YX = i - (i / chw) * chw;
-        const int Y = YX / cw, X = YX - Y * cw;
+        int YX, X;
+        const int Z = Z0 + split(i, chw, Lc.fhw, YX);
+        const int Y = split(YX, cw, Lc.fw, X);
         const int z = 2 * Z + (j >> 2), y = 2 * Y + ((j >> 1) & 1), x = 2 * X + (j & 1);
         const bool has = i < total && z < L.d && y < h && x < w;
         float term = 0.f;
@@ -1805,6 +1811,11 @@ static size_t ctail_layout(const MgHierarchy& H, int lt, int ls, int R, CtArgs* 
         L.w = (int)D.w;
         L.ppc = l < ls ? (int)((D.d + R - 1) / R) : (int)D.d;
         L.P = (int)(((size_t)L.ppc * D.h * D.w + 3) & ~(size_t)3);
+        L.fhalf = fast_div((unsigned)((D.w + 1) / 2));
+        L.fh = fast_div((unsigned)D.h);
+        L.fw = fast_div((unsigned)D.w);
+        L.fhw = fast_div((unsigned)(D.h * D.w));
+        L.fppc = fast_div((unsigned)L.ppc);
         L.off = (int)off;
         L.wx = H.lv[l].wx;
         L.wy = H.lv[l].wy;
@@ -2003,17 +2014,18 @@ static int vcycle(pg_grid* g, const MgHierarchy& H, const float* r, float* z, in
             // for 32^3 coarse cells but 14 -> 19 us for 64^3)
             const int kind = l == 0 ? KK_MG_RESTRICT : KK_MG_RESTRICT_C;
             const int cd = (int)C.D.d, ch = (int)C.D.h, cw = (int)C.D.w;
+            const FastDiv fcw = fast_div((unsigned)cw), fch = fast_div((unsigned)ch);
             cudaStream_t ss = s;
             if (nc <= kRestrictPerChild) {
                 if (l == 0)
-                    PG_LAUNCH(kind, ss, k_mg_restrict8<true><<<blocks_for(g, 8 * nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state));
+                    PG_LAUNCH(kind, ss, k_mg_restrict8<true><<<blocks_for(g, 8 * nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state, fcw, fch));
                 else
-                    PG_LAUNCH(kind, ss, k_mg_restrict8<false><<<blocks_for(g, 8 * nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state));
+                    PG_LAUNCH(kind, ss, k_mg_restrict8<false><<<blocks_for(g, 8 * nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state, fcw, fch));
             } else {
                 if (l == 0)
-                    PG_LAUNCH(kind, ss, k_mg_restrict<true><<<blocks_for(g, nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state));
+                    PG_LAUNCH(kind, ss, k_mg_restrict<true><<<blocks_for(g, nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state, fcw, fch));
                 else
-                    PG_LAUNCH(kind, ss, k_mg_restrict<false><<<blocks_for(g, nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state));
+                    PG_LAUNCH(kind, ss, k_mg_restrict<false><<<blocks_for(g, nc), kMgThreads, 0, ss>>>(v, e, f, C.f, cd, ch, cw, g->ws.state, fcw, fch));
             }
         }
     }
