@@ -489,12 +489,12 @@ static int solve_refined(pg_grid* g, const pg_solver_params* prm, float* x, cons
         const bool from_b = rounds == 0 && !guess;
         CgBuffers<float> buf{(float*)d, from_b ? b : (const float*)rin, (float*)rr, (float*)ap,
                              {(float*)p0, (float*)p1}};
-        // Round 0 of the MG path accumulates x = 0 + sum(alpha p) straight
-        // into the double-float iterate (no k_xdf_set).  An FP32 iterate
-        // floors the true residual near 2e-6 of ||b|| (the FP32 sum of a few
-        // long steps), so FP32 rounds are asked for no more than 1e-5 and a
-        // second round follows; the double-float one is asked for the
-        // target itself and usually ends the solve.
+        // The first refinement round of the MG path accumulates x = 0 +
+        // sum(alpha p) straight into the double-float iterate (no
+        // k_xdf_set).  An FP32 iterate floors the true residual near 2e-6 of
+        // ||b|| (the FP32 sum of a few long steps), so FP32 rounds are asked
+        // for no more than 1e-5 and a second round follows; the double-float
+        // one is asked for the target itself and usually ends the solve.
         bool dfx = false;
         if (from_b && !native && !hook && prm->precond == PG_PRECOND_MG) {
             CgBuffers<float> b2 = buf;
