@@ -495,6 +495,11 @@ uint32_t pg_debug_stage_wait_polls_default(void);
  * Needs at least two levels; synchronous. */
 int pg_debug_mg_vcycle_ms(pg_grid* g, double dt, int nsmooth, int reps, double* full_ms, double* coarse_ms);
 
+/* Test hook (host only, no GPU needed): the Moore-Penrose pseudo-inverse the
+ * multigrid coarsest solve uses, of the symmetric n x n row-major matrix a
+ * (overwritten; eigenvalues below 1e-10 of the largest count as zero). */
+int pg_debug_sym_pinv(int n, double* a);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,6 +104,7 @@ _SIGS = {
     "pg_debug_stage_wait_polls_default": (C.c_uint32, []),
     "pg_debug_mg_vcycle_ms": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double)]),
+    "pg_debug_sym_pinv": (C.c_int, [C.c_int, C.c_void_p]),
     "pg_last_error": (C.c_char_p, []),
     "pg_version": (_I, []),
     "pg_grid_create_2d": (_I, [_I64, _I64, C.POINTER(_P)]),

@@ -2100,6 +2100,16 @@ template int solve_mgpcg<double>(pg_grid*, const pg_solver_params*, const CgConf
 
 using namespace pg;
 
+// The coarsest level's pseudo-inverse routine on a caller's symmetric matrix
+// (host only; for tests).
+extern "C" int pg_debug_sym_pinv(int n, double* a) {
+    if (n < 1 || n > 4096 || !a) return bad_arg("pg_debug_sym_pinv: bad argument");
+    std::vector<double> m(a, a + (size_t)n * n);
+    sym_pinv(n, m);
+    std::copy(m.begin(), m.end(), a);
+    return PG_OK;
+}
+
 // Device time of one V-cycle and of its coarse part (levels >= 1), each
 // captured once into a CUDA graph and replayed `reps` times between two
 // events on a private stream; r = 0 (the kernels' work does not depend on

@@ -141,3 +141,40 @@ def test_bad_args_are_rejected(lib):
     assert L.pg_laplacian_f32(None, None, None, C.c_double(1.0)) == lib.PG_BAD_ARG
     assert L.pg_pcg_f32(None, 0, None, None, 10, C.c_double(0.1), None, None, None, C.c_double(1.0), None) \
         == lib.PG_BAD_ARG
+
+
+def test_coarsest_pseudo_inverse(lib):
+    """The multigrid coarsest solve's pseudo-inverse (host code, no GPU): on
+    a 4^3 cell Laplacian with random face weights, a solid cell and two
+    disconnected components it matches numpy's pinv to 1e-10 relative."""
+    import numpy as np
+
+    L = lib.load()
+    rng = np.random.default_rng(3)
+    d = h = w = 4
+    n = d * h * w
+    a = np.zeros((n, n))
+
+    def link(c, k, wt):
+        a[c, c] += wt
+        a[k, k] += wt
+        a[c, k] -= wt
+        a[k, c] -= wt
+
+    for z in range(d):
+        for y in range(h):
+            for x in range(w):
+                c = (z * h + y) * w + x
+                for ok, k in ((x > 0, c - 1), (y > 0, c - w), (z > 0, c - h * w)):
+                    if not ok:
+                        continue
+                    wt = float(rng.choice([0.0, 0.5, 1.0, 1.5, 2.0]))
+                    if 21 in (c, k) or (z == 2) != (k // (h * w) == 2):  # a solid cell; z = 2 cut off
+                        wt = 0.0
+                    link(c, k, wt)
+    m = np.ascontiguousarray(a.copy())
+    assert L.pg_debug_sym_pinv(n, m.ctypes.data) == 0
+    want = np.linalg.pinv(a, rcond=1e-10, hermitian=True)
+    assert np.abs(m - want).max() <= 1e-10 * np.abs(want).max()
+    with pytest.raises(Exception):
+        lib.check(L.pg_debug_sym_pinv(0, m.ctypes.data))
