@@ -822,9 +822,12 @@ static int run_cg_pm(pg_grid* g, const CgConfig& cfg, CgBuffers<T> buf, pg_pcg_s
         pending = slot;
         slot ^= 1;
     }
+    static_assert(sizeof(CgState) % 4 == 0, "CgState words");
+    k_words_out<<<1, 64, 0, s>>>((const unsigned*)ws.state, (unsigned*)(ws.state_host + 2),
+                                 (int)(sizeof(CgState) / 4));
+    PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(s));
-    CgState st;
-    PG_CUDA(cudaMemcpy(&st, ws.state, sizeof(CgState), cudaMemcpyDeviceToHost));
+    const CgState st = ws.state_host[2];
     if (G) prof_add_launches((int64_t)G->body_kernels * std::max<i64>(st.iter, 1));
     if (stats) {
         stats->iterations = st.iter;

@@ -20,13 +20,19 @@ int cuda_fail(cudaError_t e, const char* what) {
     return PG_CUDA_ERROR;
 }
 
+__global__ void k_words_out(const unsigned* __restrict__ src, unsigned* dst, int nwords) {
+    for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+}
+
 int ensure_workspace(pg_grid* g) {
     Workspace& ws = g->ws;
     if (ws.state) return PG_OK;
     PG_CUDA(cudaMalloc(&ws.partials, sizeof(double) * 4 * kMaxBlocks));
     PG_CUDA(cudaMalloc(&ws.state, sizeof(CgState)));
     PG_CUDA(cudaMemset(ws.state, 0, sizeof(CgState)));
-    PG_CUDA(cudaMallocHost(&ws.state_host, 2 * sizeof(CgState)));
+    // slots 0, 1: the host-polled loop; slot 2: the final state; then one
+    // double (a reduction result read back by the host)
+    PG_CUDA(cudaMallocHost(&ws.state_host, 3 * sizeof(CgState) + sizeof(double)));
     PG_CUDA(cudaEventCreateWithFlags(&ws.ev[0], cudaEventDisableTiming));
     PG_CUDA(cudaEventCreateWithFlags(&ws.ev[1], cudaEventDisableTiming));
     return PG_OK;

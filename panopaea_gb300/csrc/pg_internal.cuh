@@ -156,7 +156,7 @@ struct CgState {
 struct Workspace {
     double* partials = nullptr;  // per-block reduction partials (4 x kMaxBlocks: two reductions of two kernels)
     CgState* state = nullptr;    // device
-    CgState* state_host = nullptr;  // pinned mirror
+    CgState* state_host = nullptr;  // pinned mirror (see ensure_workspace)
     void* vec = nullptr;         // extra CG vectors (lazily sized)
     size_t vec_bytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -266,6 +266,13 @@ void release_pockets(Pockets* pk);
 void pocket_project(cudaStream_t s, float* a, const Pockets& pk);
 
 int ensure_workspace(pg_grid* g);
+
+// Small results for the host are written into pinned host memory by a
+// one-block kernel at the end of the stream's work instead of copied by the
+// copy engine, whose queue may hold a caller's large transfers on other
+// streams.
+__global__ void k_words_out(const unsigned* __restrict__ src, unsigned* dst, int nwords);
+inline double* host_scalar(Workspace& ws) { return (double*)(ws.state_host + 3); }
 void release_extras(pg_grid* g);
 int ensure_vec(pg_grid* g, size_t bytes);
 

@@ -339,6 +339,7 @@ __global__ void k_xdf_store(float* __restrict__ out, const float* __restrict__ x
 // x64 is a double array (native) or the [xh | xl] pair (double-float).
 static int residual64(pg_grid* g, const float* b, const void* x64, bool native, double dt, float* r,
                       double* rmax_host) {
+    if (const int rc = ensure_workspace(g)) return rc;
     Extras* ex = extras_of(g);
     const Dims& D = g->dims;
     const int nb = grid_blocks(g, D.nc(), kThreads, 8);
@@ -375,8 +376,11 @@ static int residual64(pg_grid* g, const float* b, const void* x64, bool native, 
         }
     }
     PG_CHECK_LAUNCH();
-    PG_CUDA(cudaMemcpyAsync(rmax_host, dev_out, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+    double* hs = host_scalar(g->ws);
+    k_words_out<<<1, 32, 0, g->stream>>>((const unsigned*)dev_out, (unsigned*)hs, 2);
+    PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(g->stream));
+    *rmax_host = *hs;
     return PG_OK;
 }
 
