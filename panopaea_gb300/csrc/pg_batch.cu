@@ -622,7 +622,7 @@ static std::string tune_key(const pg_batch* B) {
         hsh = (hsh ^ (unsigned long long)B->h[g]) * 1099511628211ull;
         hsh = (hsh ^ (unsigned long long)B->w[g]) * 1099511628211ull;
     }
-    char buf[256];
+    char buf[sizeof prop.name + 64];
     snprintf(buf, sizeof buf, "%s|sm%d%d|n%d|%016llx", prop.name, prop.major, prop.minor, B->n, hsh);
     std::string k(buf);
     for (auto& ch : k)

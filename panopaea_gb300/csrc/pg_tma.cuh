@@ -150,7 +150,7 @@ inline int zwalk_blocks(int ntiles, i64 d, int cap) {
 }
 
 // Host: encode a 3D tiled map over a dense (d, h, w) array of elem-byte
-// elements with box (bx, by, 1); false when the driver rejects it (base,
+// elements with box (bx, by, 1); false when the CUDA driver rejects it (base,
 // stride or box alignment) -- callers then use their non-TMA path.
 bool encode_map_3d(CUtensorMap* map, const void* base, int elem, i64 w, i64 h, i64 d, int bx, int by);
 
