@@ -390,6 +390,42 @@ int pg_wavelet_div_coeff_2d(int levels, const double* vx, const double* vy, doub
 int pg_wavelet_inv_div_coeff_2d(int levels, const double* div, const double* n, double* vx, double* vy, int64_t h,
                                 int64_t w, void* cuda_stream);
 
+/* Border variants (mod.rs:454-681): zero sampling outside a line, bands of
+ * s / 2 + 2 B samples for an s-sample line (B = the filter length: 2 Haar,
+ * 6 Bior13 and Bior22, 10 Bior24, 4 Bior31), so the transform is larger
+ * than its input and the inverse reconstructs the input's leading samples.
+ * A transform is one packed FP64 array: the coarse band, then per level
+ * (finest first) its detail band (1D) or its three detail bands lyhx,
+ * hylx, hyhx (2D, each row-major) -- the (coarse, details) pair the
+ * reference returns.  The sizes functions run on the host only (no CUDA
+ * call): `packed` elements of the transform, `temp` elements of the
+ * scratch array the transforms need (0: none; temp may then be NULL) and
+ * the inverse's output length (1D: coarse + detail - 4 B per level) or
+ * shape (2D: 2 coarse - 4 B per level), -1 where that arithmetic goes below
+ * zero at some level (tiny inputs, many levels: the reference's unsigned
+ * sizes underflow there) and the inverse returns PG_BAD_ARG.  Input, output
+ * and temp must not overlap.  n, h, w >= 2; levels 0..40. */
+int pg_wavelet_border_sizes_1d(int wavelet, int64_t n, int levels, int64_t* packed, int64_t* temp,
+                               int64_t* inverse_n);
+int pg_wavelet_border_sizes_2d(int wavelet_x, int wavelet_y, int64_t h, int64_t w, int levels, int64_t* packed,
+                               int64_t* temp, int64_t* inverse_h, int64_t* inverse_w);
+/* fwt_1d_border / ifwt_1d_border (mod.rs:454-486); the inverse takes the
+ * forward's n and levels (n and n + 1 give the same bands for even n). */
+int pg_wavelet_fwt_1d_border(int wavelet, const double* input, int64_t n, int levels, double* packed, double* temp,
+                             void* cuda_stream);
+int pg_wavelet_ifwt_1d_border(int wavelet, const double* packed, int64_t n, int levels, double* output, double* temp,
+                              void* cuda_stream);
+/* fwt_2d_separate_isotropic_border / ifwt_2d_separate_isotropic_border
+ * (mod.rs:551-641): x then y forward, y then x inverse. */
+int pg_wavelet_fwt_2d_border(int wavelet_x, int wavelet_y, const double* input, int64_t h, int64_t w, int levels,
+                             double* packed, double* temp, void* cuda_stream);
+int pg_wavelet_ifwt_2d_border(int wavelet_x, int wavelet_y, const double* packed, int64_t h, int64_t w, int levels,
+                              double* output, double* temp, void* cuda_stream);
+/* div_coeff_2d_border (mod.rs:645-681) of two packed 2D border transforms of
+ * (h, w) inputs: the packed div and n transforms. */
+int pg_wavelet_div_coeff_2d_border(int wavelet_x, int wavelet_y, const double* vx, const double* vy, int64_t h,
+                                   int64_t w, int levels, double* div, double* n, void* cuda_stream);
+
 /* ----------------------------------------------------------------------- */
 /* Learned pressure guess (extension, no reference counterpart: panopaea has
  * no learned component).  A 3-level 3D conv U-Net, 16 base channels, BF16

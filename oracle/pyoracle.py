@@ -422,3 +422,105 @@ def wavelet_inv_div_coeff_2d(levels, dv, nn):
     h, w = dv.shape
     _wcall("wvo_inv_div_coeff_2d", int(levels), _p(dv), _p(nn), _p(vx), _p(vy), C.c_long(h), C.c_long(w))
     return vx, vy
+
+
+# Border variants (mod.rs:454-681).  A transform is (coarse, details): 1D
+# details a list of arrays (finest first), 2D a list of [lyhx, hylx, hyhx].
+WAVELET_TAPS = (2, 6, 6, 10, 4)  # filter length = border width of each wavelet
+
+
+def wavelet_border_bands(s, levels, wavelet):
+    """Band lengths s_{k+1} = s_k // 2 + 2 * border width, finest first."""
+    out = []
+    for _ in range(levels):
+        s = s // 2 + 2 * WAVELET_TAPS[wavelet]
+        out.append(s)
+    return out
+
+
+def wavelet_fwt_1d_border(wavelet, data, levels):
+    x = np.ascontiguousarray(data, np.float64)
+    b = wavelet_border_bands(x.size, levels, wavelet)
+    packed = np.zeros((b[-1] if levels else x.size) + sum(b))
+    _wcall("wvo_fwt_1d_border", int(wavelet), _p(x), C.c_long(x.size), int(levels), _p(packed))
+    coarse, off, details = packed[:packed.size - sum(b)], packed.size - sum(b), []
+    for n in b:
+        details.append(packed[off:off + n])
+        off += n
+    return coarse, details
+
+
+def wavelet_ifwt_1d_border(wavelet, transform, n):
+    """ifwt_1d_border of the fwt_1d_border of a length-n input."""
+    coarse, details = transform
+    packed = np.ascontiguousarray(np.concatenate([coarse] + list(details)), np.float64)
+    out = np.zeros(packed.size + n)
+    fn = lib().wvo_ifwt_1d_border
+    fn.restype = C.c_long
+    m = fn(int(wavelet), _p(packed), C.c_long(n), int(len(details)), _p(out))
+    return out[:m]
+
+
+def wavelet_fwt_2d_border(wx, wy, data, levels):
+    x = np.ascontiguousarray(data, np.float64)
+    h, w = x.shape
+    br, bc = wavelet_border_bands(h, levels, wy), wavelet_border_bands(w, levels, wx)
+    cshape = (br[-1], bc[-1]) if levels else (h, w)
+    total = cshape[0] * cshape[1] + sum(3 * r * c for r, c in zip(br, bc))
+    packed = np.zeros(total)
+    _wcall("wvo_fwt_2d_border", int(wx), int(wy), _p(x), C.c_long(h), C.c_long(w), int(levels), _p(packed))
+    return _unpack2(packed, cshape, br, bc)
+
+
+def _unpack2(packed, cshape, br, bc):
+    off = cshape[0] * cshape[1]
+    coarse, details = packed[:off].reshape(cshape), []
+    for r, c in zip(br, bc):
+        band = []
+        for _ in range(3):
+            band.append(packed[off:off + r * c].reshape(r, c))
+            off += r * c
+        details.append(band)
+    return coarse, details
+
+
+def _pack2(transform):
+    coarse, details = transform
+    return np.ascontiguousarray(np.concatenate([np.ravel(coarse)] + [np.ravel(a) for d in details for a in d]),
+                                np.float64)
+
+
+def wavelet_border_inverse_shape(wx, wy, h, w, levels):
+    """Shape of ifwt_2d_separate_isotropic_border of the forward transform
+    of an (h, w) input: per level 2 * coarse - 4 * border width."""
+    br, bc = wavelet_border_bands(h, levels, wy), wavelet_border_bands(w, levels, wx)
+    r, c = (br[-1], bc[-1]) if levels else (h, w)
+    for _ in range(levels):
+        r, c = 2 * r - 4 * WAVELET_TAPS[wy], 2 * c - 4 * WAVELET_TAPS[wx]
+    return r, c
+
+
+def wavelet_ifwt_2d_border(wx, wy, transform, h, w):
+    """ifwt_2d_separate_isotropic_border of the forward transform of an (h, w) input."""
+    levels = len(transform[1])
+    packed = _pack2(transform)
+    shape = wavelet_border_inverse_shape(wx, wy, h, w, levels)
+    out = np.zeros(shape)
+    fn = lib().wvo_ifwt_2d_border
+    fn.restype = C.c_long
+    m = fn(int(wx), int(wy), _p(packed), C.c_long(h), C.c_long(w), int(levels), _p(out))
+    assert m == out.size
+    return out
+
+
+def wavelet_div_coeff_2d_border(wx, wy, tvx, tvy, h, w):
+    """div_coeff_2d_border of two forward transforms of (h, w) inputs:
+    returns the (div, n) transforms."""
+    levels = len(tvx[1])
+    a, b = _pack2(tvx), _pack2(tvy)
+    d, n = np.zeros_like(a), np.zeros_like(a)
+    _wcall("wvo_div_coeff_2d_border", int(wx), int(wy), _p(a), _p(b), C.c_long(h), C.c_long(w), int(levels), _p(d),
+           _p(n))
+    br, bc = wavelet_border_bands(h, levels, wy), wavelet_border_bands(w, levels, wx)
+    cshape = np.shape(tvx[0])
+    return _unpack2(d, cshape, br, bc), _unpack2(n, cshape, br, bc)

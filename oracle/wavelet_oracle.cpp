@@ -1,10 +1,12 @@
 // wavelet_oracle.cpp -- CPU restatement of panopaea/src/math/wavelet
-// (mod.rs:1-451, filters haar.rs:6-9 and spline.rs), TEST INFRASTRUCTURE
+// (mod.rs:1-681, filters haar.rs:6-9 and spline.rs), TEST INFRASTRUCTURE
 // ONLY: the GPU transforms of panopaea_gb300/csrc/pg_wavelet.cu are checked
 // against it.  Loops follow the reference as written: down_convolution
 // folds with MirrorSampler (mod.rs:52-79), up_convolution scatters with the
 // wrapped index (mod.rs:81-112), and the level loops, temporaries and axis
-// orders of fwt_1d ... div_coeff_2d, inv_div_coeff_2d (mod.rs:114-451).
+// orders of fwt_1d ... div_coeff_2d, inv_div_coeff_2d (mod.rs:114-451), and
+// the border variants fwt_1d_border ... div_coeff_2d_border (mod.rs:454-681).
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <initializer_list>
@@ -259,4 +261,226 @@ WVO_EXPORT void wvo_inv_div_coeff_2d(int levels, const double* dv, const double*
         r *= 2;
         c *= 2;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Border variants (mod.rs:454-681): zero sampling, bands of s / 2 + 2 B
+// samples (B = the border width, the filter length), the forward down
+// convolution shifted by B bands and the inverse scatter shifted back by 2 B.
+// Transforms are packed into one array: the coarse band, then per level
+// (finest first) its detail band(s) -- 1D: detail; 2D: lyhx, hylx, hyhx
+// (the [detail_lyhx, detail_hylx, detail_hyhx] order of mod.rs:594).
+
+namespace {
+
+double zero_fetch(const Line& in, idx i) { return i >= 0 && i < in.len ? in[i] : 0.0; }  // mod.rs:26-35
+
+void down_convolution_border(const Filt& W, const Line& in, const Line& coarse, const Line& detail) {  // mod.rs:488-514
+    const idx n = W.n, fh = n / 2, bw = n, half = detail.len;
+    for (idx i = 0; i < half; ++i) {
+        double acc = 0.0;
+        for (idx f = 0; f < n; ++f) acc = zero_fetch(in, 2 * (i - bw) + f - fh + 1) * W.dl[n - 1 - f] + acc;
+        coarse[i] = acc;
+    }
+    for (idx i = 0; i < half; ++i) {
+        double acc = 0.0;
+        for (idx f = 0; f < n; ++f) acc = zero_fetch(in, 2 * (i - bw) + f - fh + 1) * W.dh[n - 1 - f] + acc;
+        detail[i] = acc;
+    }
+}
+
+void up_convolution_border(const Filt& W, const Line& coarse, const Line& detail, const Line& out) {  // mod.rs:516-549
+    const idx n = W.n, len = coarse.len + detail.len, half = len / 2, fh = n / 2, bw = n;
+    for (idx k = 0; k < out.len; ++k) out[k] = 0.0;
+    for (idx i = 0; i < half; ++i)
+        for (idx f = 0; f < n; ++f) {
+            const idx id = 2 * i + f - fh + 1;
+            const idx o = (id < 0 ? (id + len) % len : id % len) - 2 * bw;
+            if (o < 0 || o >= out.len) continue;
+            out[o] += zero_fetch(coarse, i) * W.ul[f] + zero_fetch(detail, i) * W.uh[f];
+        }
+}
+
+struct Arr2 {
+    idx r = 0, c = 0;
+    std::vector<double> v;
+    Arr2() = default;
+    Arr2(idx r_, idx c_) : r(r_), c(c_), v(r_ * c_, 0.0) {}
+    Line row(idx i) { return Line{v.data() + i * c, 1, c}; }
+    Line col(idx j) { return Line{v.data() + j, c, r}; }
+};
+
+// fwt_1d_border (mod.rs:454-472)
+void fwt1b(const Filt& W, std::vector<double> coarse, int levels, std::vector<double>* out_coarse,
+           std::vector<std::vector<double>>* details) {
+    for (int k = 0; k < levels; ++k) {
+        const idx band = (idx)coarse.size() / 2 + 2 * W.n;
+        std::vector<double> detail(band), down(band);
+        down_convolution_border(W, Line{coarse.data(), 1, (idx)coarse.size()}, Line{down.data(), 1, band},
+                                Line{detail.data(), 1, band});
+        details->push_back(detail);
+        coarse = down;
+    }
+    *out_coarse = coarse;
+}
+
+// fwt_2d_separate_isotropic_border (mod.rs:551-597)
+void fwt2b(const Filt& Wx, const Filt& Wy, Arr2 coarse, int levels, Arr2* out_coarse, std::vector<Arr2>* details) {
+    for (int k = 0; k < levels; ++k) {
+        const idx br = coarse.r / 2 + 2 * Wy.n, bc = coarse.c / 2 + 2 * Wx.n;
+        Arr2 down_lx(coarse.r, bc), detail_hx(coarse.r, bc), lyhx(br, bc), hylx(br, bc), hyhx(br, bc), down(br, bc);
+        for (idx i = 0; i < coarse.r; ++i) down_convolution_border(Wx, coarse.row(i), down_lx.row(i), detail_hx.row(i));
+        for (idx i = 0; i < bc; ++i) {
+            down_convolution_border(Wy, down_lx.col(i), down.col(i), hylx.col(i));
+            down_convolution_border(Wy, detail_hx.col(i), lyhx.col(i), hyhx.col(i));
+        }
+        coarse = down;
+        details->push_back(lyhx);
+        details->push_back(hylx);
+        details->push_back(hyhx);
+    }
+    *out_coarse = coarse;
+}
+
+// ifwt_2d_separate_isotropic_border (mod.rs:599-641): y, then x
+Arr2 ifwt2b(const Filt& Wx, const Filt& Wy, Arr2 coarse, std::vector<Arr2>& details, int levels) {
+    for (int k = levels - 1; k >= 0; --k) {
+        Arr2& lyhx = details[3 * k];
+        Arr2& hylx = details[3 * k + 1];
+        Arr2& hyhx = details[3 * k + 2];
+        const idx ur = 2 * coarse.r - 4 * Wy.n, uc = 2 * coarse.c - 4 * Wx.n;
+        Arr2 up(ur, uc), up_lx(ur, coarse.c), detail_hx(ur, coarse.c);
+        for (idx i = 0; i < coarse.c; ++i) {
+            up_convolution_border(Wy, coarse.col(i), hylx.col(i), up_lx.col(i));
+            up_convolution_border(Wy, lyhx.col(i), hyhx.col(i), detail_hx.col(i));
+        }
+        for (idx i = 0; i < ur; ++i) up_convolution_border(Wx, up_lx.row(i), detail_hx.row(i), up.row(i));
+        coarse = up;
+    }
+    return coarse;
+}
+
+// Band sizes of the forward transforms: s_{k+1} = s_k / 2 + 2 B.
+std::vector<idx> bands(idx s, int levels, idx bw) {
+    std::vector<idx> b;
+    for (int k = 0; k < levels; ++k) {
+        s = s / 2 + 2 * bw;
+        b.push_back(s);
+    }
+    return b;
+}
+
+}  // namespace
+
+WVO_EXPORT void wvo_fwt_1d_border(int wavelet, const double* in, long n, int levels, double* packed) {
+    const Filt W = filt(wavelet);
+    std::vector<double> coarse;
+    std::vector<std::vector<double>> details;
+    fwt1b(W, std::vector<double>(in, in + n), levels, &coarse, &details);
+    for (double v : coarse) *packed++ = v;
+    for (auto& d : details)
+        for (double v : d) *packed++ = v;
+}
+
+// ifwt_1d_border (mod.rs:474-486) of a packed fwt_1d_border of length n
+WVO_EXPORT long wvo_ifwt_1d_border(int wavelet, const double* packed, long n, int levels, double* out) {
+    const Filt W = filt(wavelet);
+    const std::vector<idx> b = bands(n, levels, W.n);
+    std::vector<double> coarse(packed, packed + (levels ? b.back() : n));
+    const double* p = packed + coarse.size();
+    std::vector<const double*> dp;
+    for (int k = 0; k < levels; ++k) {
+        dp.push_back(p);
+        p += b[k];
+    }
+    for (int k = levels - 1; k >= 0; --k) {
+        const idx len = (idx)coarse.size() + b[k];
+        std::vector<double> up(len - 4 * W.n);
+        up_convolution_border(W, Line{coarse.data(), 1, (idx)coarse.size()}, Line{(double*)dp[k], 1, b[k]},
+                              Line{up.data(), 1, (idx)up.size()});
+        coarse = up;
+    }
+    for (double v : coarse) *out++ = v;
+    return (long)coarse.size();
+}
+
+WVO_EXPORT void wvo_fwt_2d_border(int wx, int wy, const double* in, long h, long w, int levels, double* packed) {
+    const Filt Fx = filt(wx), Fy = filt(wy);
+    Arr2 x(h, w), coarse;
+    std::copy(in, in + h * w, x.v.begin());
+    std::vector<Arr2> details;
+    fwt2b(Fx, Fy, x, levels, &coarse, &details);
+    for (double v : coarse.v) *packed++ = v;
+    for (auto& d : details)
+        for (double v : d.v) *packed++ = v;
+}
+
+namespace {
+// The packed 2D transform of an (h, w) input as arrays.
+void unpack2(const Filt& Fx, const Filt& Fy, const double* packed, long h, long w, int levels, Arr2* coarse,
+             std::vector<Arr2>* details) {
+    const std::vector<idx> br = bands(h, levels, Fy.n), bc = bands(w, levels, Fx.n);
+    *coarse = levels ? Arr2(br.back(), bc.back()) : Arr2(h, w);
+    std::copy(packed, packed + coarse->v.size(), coarse->v.begin());
+    packed += coarse->v.size();
+    for (int k = 0; k < levels; ++k)
+        for (int q = 0; q < 3; ++q) {
+            Arr2 a(br[k], bc[k]);
+            std::copy(packed, packed + a.v.size(), a.v.begin());
+            packed += a.v.size();
+            details->push_back(a);
+        }
+}
+void pack2(const Arr2& coarse, const std::vector<Arr2>& details, double* packed) {
+    for (double v : coarse.v) *packed++ = v;
+    for (auto& d : details)
+        for (double v : d.v) *packed++ = v;
+}
+}  // namespace
+
+// ifwt_2d_separate_isotropic_border (mod.rs:599-641) of a packed 2D border
+// transform of an (h, w) input; returns the result's number of elements
+WVO_EXPORT long wvo_ifwt_2d_border(int wx, int wy, const double* packed, long h, long w, int levels, double* out) {
+    const Filt Fx = filt(wx), Fy = filt(wy);
+    Arr2 coarse;
+    std::vector<Arr2> details;
+    unpack2(Fx, Fy, packed, h, w, levels, &coarse, &details);
+    const Arr2 r = ifwt2b(Fx, Fy, coarse, details, levels);
+    std::copy(r.v.begin(), r.v.end(), out);
+    return (long)r.v.size();
+}
+
+// div_coeff_2d_border (mod.rs:645-681) of two packed 2D border transforms
+WVO_EXPORT void wvo_div_coeff_2d_border(int wx, int wy, const double* vxp, const double* vyp, long h, long w,
+                                        int levels, double* divp, double* np_) {
+    const Filt Fx = filt(wx), Fy = filt(wy);
+    Arr2 vxc, vyc;
+    std::vector<Arr2> vxd, vyd;
+    unpack2(Fx, Fy, vxp, h, w, levels, &vxc, &vxd);
+    unpack2(Fx, Fy, vyp, h, w, levels, &vyc, &vyd);
+    std::vector<Arr2> dd, nd;
+    for (int k = 0; k < levels; ++k) {
+        Arr2 &vx01 = vxd[3 * k], &vx10 = vxd[3 * k + 1], &vx11 = vxd[3 * k + 2];
+        Arr2 &vy01 = vyd[3 * k], &vy10 = vyd[3 * k + 1], &vy11 = vyd[3 * k + 2];
+        const idx R = vx01.r, Cc = vx01.c;
+        Arr2 d01(R, Cc), d10(R, Cc), d11(R, Cc), n01(R, Cc), n10(R, Cc), n11(R, Cc);
+        for (idx y = 0; y < R; ++y)
+            for (idx x = 0; x < Cc; ++x) {
+                const idx q = y * Cc + x, ym = (y > 0 ? y - 1 : 0) * Cc + x, xm = y * Cc + (x > 0 ? x - 1 : 0);
+                d01.v[q] = vy01.v[q];
+                d10.v[q] = vx10.v[q];
+                d11.v[q] = (vx11.v[q] - vy11.v[q]) / 2.0;
+                n01.v[q] = vx01.v[q] + (vy01.v[q] - vy01.v[ym]) / 4.0;
+                n10.v[q] = vy10.v[q] + (vx10.v[q] - vx10.v[xm]) / 4.0;
+                n11.v[q] = (vx11.v[q] + vy11.v[q]) / 2.0;
+            }
+        dd.push_back(d01);
+        dd.push_back(d10);
+        dd.push_back(d11);
+        nd.push_back(n01);
+        nd.push_back(n10);
+        nd.push_back(n11);
+    }
+    pack2(vxc, dd, divp);
+    pack2(vyc, nd, np_);
 }

@@ -141,6 +141,14 @@ _SIGS = {
     "pg_wavelet_ifwt_2d": (_I, [_I, _I, _I, _P, _I64, _I64, _I, _P, _P]),
     "pg_wavelet_div_coeff_2d": (_I, [_I, _P, _P, _P, _P, _I64, _I64, _P]),
     "pg_wavelet_inv_div_coeff_2d": (_I, [_I, _P, _P, _P, _P, _I64, _I64, _P]),
+    "pg_wavelet_border_sizes_1d": (_I, [_I, _I64, _I, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)]),
+    "pg_wavelet_border_sizes_2d": (_I, [_I, _I, _I64, _I64, _I, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64),
+                                        C.POINTER(_I64)]),
+    "pg_wavelet_fwt_1d_border": (_I, [_I, _P, _I64, _I, _P, _P, _P]),
+    "pg_wavelet_ifwt_1d_border": (_I, [_I, _P, _I64, _I, _P, _P, _P]),
+    "pg_wavelet_fwt_2d_border": (_I, [_I, _I, _P, _I64, _I64, _I, _P, _P, _P]),
+    "pg_wavelet_ifwt_2d_border": (_I, [_I, _I, _P, _I64, _I64, _I, _P, _P, _P]),
+    "pg_wavelet_div_coeff_2d_border": (_I, [_I, _I, _P, _P, _I64, _I64, _I, _P, _P, _P]),
     "pg_unet_num_params": (_I64, []),
     "pg_unet_create": (_I, [_I64, _I64, _I64, C.POINTER(_P)]),
     "pg_unet_destroy": (_I, [_P]),

@@ -1,5 +1,5 @@
 // pg_wavelet.cu -- wavelet and divergence-free wavelet transforms
-// (panopaea/src/math/wavelet/mod.rs:1-451; the filters of haar.rs and
+// (panopaea/src/math/wavelet/mod.rs:1-681; the filters of haar.rs and
 // spline.rs).  The reference marks the module as early, mostly abandoned
 // tests; its behaviour is restated as written, boundary rules included.
 //
@@ -15,73 +15,22 @@
 // those of fwt_1d / ifwt_1d / fwt_2d_isotropic / ifwt_2d_isotropic /
 // fwt_2d_separate_isotropic / ifwt_2d_separate_isotropic /
 // fwt_2d_anisotropic (mod.rs:114-294); div_coeff_2d / inv_div_coeff_2d
-// (mod.rs:296-451) are one launch per level.
+// (mod.rs:296-451) are one launch per level.  The border variants
+// (mod.rs:454-681) run the passes of pg_wavelet_border.cuh: one launch per
+// 1D pass over every line of a band, into a packed output.
 #include <algorithm>
-#include <initializer_list>
 
 #include "pg_internal.cuh"
+#include "pg_wavelet_border.cuh"
 
 namespace pg {
 
 namespace {
 
 constexpr int kWThreads = 256;
-constexpr int kMaxTaps = 10;
-
-struct WFilter {
-    int n;
-    double down_low[kMaxTaps], down_high[kMaxTaps], up_low[kMaxTaps], up_high[kMaxTaps];
-};
-
-// The filter tables of haar.rs:6-9 and spline.rs (bior 1.3, 2.2, 2.4, 3.1).
-constexpr double kS = 0.70710678118654752440084436210484903;
-constexpr double kA = 0.08838834764831844055010554526310612;
-constexpr double kB = 0.35355339059327376220042218105242451;
-constexpr double kC = 0.17677669529663688110021109052621225;
-constexpr double kD = 1.06066017177982128660126654315727355;
-constexpr double kE = 0.5303300858899107;
-constexpr double kF = 0.03314563036811942;
-constexpr double kG = 0.06629126073623884;
-constexpr double kH = 0.4198446513295126;
-constexpr double kI = 0.9943689110435825;
-
-bool filter_of(int wavelet, WFilter* out) {
-    WFilter f{};
-    auto set = [&](int n, std::initializer_list<double> ul, std::initializer_list<double> uh,
-                   std::initializer_list<double> dl, std::initializer_list<double> dh) {
-        f.n = n;
-        int k = 0;
-        for (double v : ul) f.up_low[k++] = v;
-        k = 0;
-        for (double v : uh) f.up_high[k++] = v;
-        k = 0;
-        for (double v : dl) f.down_low[k++] = v;
-        k = 0;
-        for (double v : dh) f.down_high[k++] = v;
-    };
-    switch (wavelet) {
-        case PG_WAVELET_HAAR:
-            set(2, {kS, kS}, {kS, -kS}, {kS, kS}, {-kS, kS});
-            break;
-        case PG_WAVELET_BIOR13:
-            set(6, {0, 0, kS, kS, 0, 0}, {-kA, -kA, kS, -kS, kA, kA}, {-kA, kA, kS, kS, kA, -kA}, {0, 0, -kS, kS, 0, 0});
-            break;
-        case PG_WAVELET_BIOR22:
-            set(6, {0, kB, kS, kB, 0, 0}, {0, kC, kB, -kD, kB, kC}, {0, -kC, kB, kD, kB, -kC}, {0, kB, -kS, kB, 0, 0});
-            break;
-        case PG_WAVELET_BIOR24:
-            set(10, {0, 0, 0, kB, kS, kB, 0, 0, 0, 0}, {0, -kF, -kG, kC, kH, -kI, kH, kC, -kG, -kF},
-                {0, kF, -kG, -kC, kH, kI, kH, -kC, -kG, kF}, {0, 0, 0, kB, -kS, kB, 0, 0, 0, 0});
-            break;
-        case PG_WAVELET_BIOR31:
-            set(4, {kC, kE, kE, kC}, {-kB, -kD, kD, kB}, {-kB, kD, kD, -kB}, {-kC, kE, -kE, kC});
-            break;
-        default:
-            return false;
-    }
-    *out = f;
-    return true;
-}
+using wv::filter_of;
+using wv::kMaxTaps;
+using wv::WFilter;
 
 // mod.rs:38-48 MirrorSampler::fetch
 __device__ __forceinline__ double mirror(const double* line, i64 stride, i64 len, i64 idx) {
@@ -209,6 +158,33 @@ __global__ void k_inv_div_coeff(const double* __restrict__ dv, const double* __r
     }
 }
 
+// Border variants: one thread per output sample of a pass.
+__global__ void __launch_bounds__(kWThreads) k_wdown_border(const double* __restrict__ src, wv::WLines in, double* lo,
+                                                            double* hi, wv::WLines out, WFilter F) {
+    const i64 total = in.lines * 2 * out.len;
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (i64)gridDim.x * blockDim.x)
+        wv::wdown_border_at(src, in, lo, hi, out, F, t);
+}
+
+__global__ void __launch_bounds__(kWThreads) k_wup_border(const double* __restrict__ cs, wv::WLines c,
+                                                          const double* __restrict__ ds, wv::WLines d,
+                                                          double* __restrict__ dst, wv::WLines out, WFilter F) {
+    const i64 total = out.lines * out.len;
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (i64)gridDim.x * blockDim.x)
+        wv::wup_border_at(cs, c, ds, d, dst, out, F, t);
+}
+
+__global__ void __launch_bounds__(kWThreads) k_wdiv_border(const double* __restrict__ vx, const double* __restrict__ vy,
+                                                           double* __restrict__ dv, double* __restrict__ nn, i64 R,
+                                                           i64 C) {
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < R * C; t += (i64)gridDim.x * blockDim.x)
+        wv::wdiv_border_at(vx, vy, dv, nn, R, C, t);
+}
+
+__global__ void k_wcopy_flat(const double* __restrict__ src, double* __restrict__ dst, i64 n) {
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) dst[t] = src[t];
+}
+
 int wblocks(i64 n) { return (int)std::max<i64>(1, std::min<i64>((n + kWThreads - 1) / kWThreads, 4096)); }
 
 int down(cudaStream_t s, const double* src, double* dst, i64 lines, i64 len, i64 ls, i64 es, const WFilter& F) {
@@ -236,6 +212,37 @@ int check_levels(i64 n, int levels, const WFilter& F) {
     if (levels > 0 && (n >> (levels - 1)) < F.n) return bad_arg("wavelet: the last level is shorter than the filter");
     return PG_OK;
 }
+
+// The device executor of the border passes.
+struct DeviceExec {
+    cudaStream_t s;
+    int down(const double* src, wv::WLines in, double* lo, double* hi, wv::WLines out, const WFilter& F) {
+        PG_LAUNCH(KK_DEC_OP, s,
+                  k_wdown_border<<<wblocks(in.lines * 2 * out.len), kWThreads, 0, s>>>(src, in, lo, hi, out, F));
+        PG_CHECK_LAUNCH();
+        return PG_OK;
+    }
+    int up(const double* c, wv::WLines cl, const double* d, wv::WLines dl, double* dst, wv::WLines out,
+           const WFilter& F) {
+        if (out.lines * out.len == 0) return PG_OK;
+        PG_LAUNCH(KK_DEC_OP, s, k_wup_border<<<wblocks(out.lines * out.len), kWThreads, 0, s>>>(c, cl, d, dl, dst, out, F));
+        PG_CHECK_LAUNCH();
+        return PG_OK;
+    }
+    int div(const double* vx, const double* vy, double* dv, double* nn, i64 R, i64 C) {
+        PG_LAUNCH(KK_DEC_OP, s, k_wdiv_border<<<wblocks(R * C), kWThreads, 0, s>>>(vx, vy, dv, nn, R, C));
+        PG_CHECK_LAUNCH();
+        return PG_OK;
+    }
+    int copy(const double* src, double* dst, i64 n) {
+        PG_LAUNCH(KK_DEC_OP, s, k_wcopy_flat<<<wblocks(n), kWThreads, 0, s>>>(src, dst, n));
+        PG_CHECK_LAUNCH();
+        return PG_OK;
+    }
+};
+
+// Distinct, non-overlapping device ranges [p, p + n) (n in doubles).
+bool disjoint(const double* a, i64 na, const double* b, i64 nb) { return a + na <= b || b + nb <= a; }
 
 }  // namespace
 }  // namespace pg
@@ -364,6 +371,109 @@ int pg_wavelet_inv_div_coeff_2d(int levels, const double* div, const double* n, 
     }
     PG_CHECK_LAUNCH();
     return PG_OK;
+}
+
+int pg_wavelet_border_sizes_1d(int wavelet, int64_t n, int levels, int64_t* packed, int64_t* temp,
+                               int64_t* inverse_n) {
+    WFilter F;
+    wv::Plan1d P;
+    if (!filter_of(wavelet, &F)) return bad_arg("pg_wavelet_border_sizes_1d: unknown wavelet");
+    if (!wv::plan_1d(F, n, levels, &P)) return bad_arg("pg_wavelet_border_sizes_1d: n must be >= 2, levels in 0..40");
+    if (packed) *packed = P.packed;
+    if (temp) *temp = P.temp;
+    if (inverse_n) *inverse_n = P.inverse_n;
+    return PG_OK;
+}
+
+int pg_wavelet_border_sizes_2d(int wavelet_x, int wavelet_y, int64_t h, int64_t w, int levels, int64_t* packed,
+                               int64_t* temp, int64_t* inverse_h, int64_t* inverse_w) {
+    WFilter Fx, Fy;
+    wv::Plan2d P;
+    if (!filter_of(wavelet_x, &Fx) || !filter_of(wavelet_y, &Fy))
+        return bad_arg("pg_wavelet_border_sizes_2d: unknown wavelet");
+    if (!wv::plan_2d(Fx, Fy, h, w, levels, &P))
+        return bad_arg("pg_wavelet_border_sizes_2d: h and w must be >= 2, levels in 0..40");
+    if (packed) *packed = P.packed;
+    if (temp) *temp = P.temp;
+    if (inverse_h) *inverse_h = P.inverse_h;
+    if (inverse_w) *inverse_w = P.inverse_w;
+    return PG_OK;
+}
+
+int pg_wavelet_fwt_1d_border(int wavelet, const double* input, int64_t n, int levels, double* packed, double* temp,
+                             void* stream) {
+    WFilter F;
+    wv::Plan1d P;
+    if (!filter_of(wavelet, &F)) return bad_arg("pg_wavelet_fwt_1d_border: unknown wavelet");
+    if (!wv::plan_1d(F, n, levels, &P)) return bad_arg("pg_wavelet_fwt_1d_border: n must be >= 2, levels in 0..40");
+    if (!input || !packed || (P.temp && !temp) || !disjoint(input, n, packed, P.packed) ||
+        (P.temp && (!disjoint(input, n, temp, P.temp) || !disjoint(packed, P.packed, temp, P.temp))))
+        return bad_arg("pg_wavelet_fwt_1d_border: input, packed and temp must be distinct arrays");
+    DeviceExec ex{(cudaStream_t)stream};
+    return wv::run_fwt_1d(ex, F, P, input, packed, temp);
+}
+
+int pg_wavelet_ifwt_1d_border(int wavelet, const double* packed, int64_t n, int levels, double* output, double* temp,
+                              void* stream) {
+    WFilter F;
+    wv::Plan1d P;
+    if (!filter_of(wavelet, &F)) return bad_arg("pg_wavelet_ifwt_1d_border: unknown wavelet");
+    if (!wv::plan_1d(F, n, levels, &P)) return bad_arg("pg_wavelet_ifwt_1d_border: n must be >= 2, levels in 0..40");
+    if (!P.inv_ok) return bad_arg("pg_wavelet_ifwt_1d_border: the inverse's length goes below zero at a level");
+    if (!packed || (P.inverse_n && !output) || (P.temp && !temp) || !disjoint(packed, P.packed, output, P.inverse_n) ||
+        (P.temp && (!disjoint(packed, P.packed, temp, P.temp) || !disjoint(output, P.inverse_n, temp, P.temp))))
+        return bad_arg("pg_wavelet_ifwt_1d_border: packed, output and temp must be distinct arrays");
+    DeviceExec ex{(cudaStream_t)stream};
+    return wv::run_ifwt_1d(ex, F, P, packed, output, temp);
+}
+
+int pg_wavelet_fwt_2d_border(int wavelet_x, int wavelet_y, const double* input, int64_t h, int64_t w, int levels,
+                             double* packed, double* temp, void* stream) {
+    WFilter Fx, Fy;
+    wv::Plan2d P;
+    if (!filter_of(wavelet_x, &Fx) || !filter_of(wavelet_y, &Fy))
+        return bad_arg("pg_wavelet_fwt_2d_border: unknown wavelet");
+    if (!wv::plan_2d(Fx, Fy, h, w, levels, &P))
+        return bad_arg("pg_wavelet_fwt_2d_border: h and w must be >= 2, levels in 0..40");
+    const i64 nin = h * w;
+    if (!input || !packed || (P.temp && !temp) || !disjoint(input, nin, packed, P.packed) ||
+        (P.temp && (!disjoint(input, nin, temp, P.temp) || !disjoint(packed, P.packed, temp, P.temp))))
+        return bad_arg("pg_wavelet_fwt_2d_border: input, packed and temp must be distinct arrays");
+    DeviceExec ex{(cudaStream_t)stream};
+    return wv::run_fwt_2d(ex, Fx, Fy, P, input, packed, temp);
+}
+
+int pg_wavelet_ifwt_2d_border(int wavelet_x, int wavelet_y, const double* packed, int64_t h, int64_t w, int levels,
+                              double* output, double* temp, void* stream) {
+    WFilter Fx, Fy;
+    wv::Plan2d P;
+    if (!filter_of(wavelet_x, &Fx) || !filter_of(wavelet_y, &Fy))
+        return bad_arg("pg_wavelet_ifwt_2d_border: unknown wavelet");
+    if (!wv::plan_2d(Fx, Fy, h, w, levels, &P))
+        return bad_arg("pg_wavelet_ifwt_2d_border: h and w must be >= 2, levels in 0..40");
+    if (!P.inv_ok) return bad_arg("pg_wavelet_ifwt_2d_border: the inverse's size goes below zero at a level");
+    const i64 nout = P.inverse_h * P.inverse_w;
+    if (!packed || (nout && !output) || (P.temp && !temp) || !disjoint(packed, P.packed, output, nout) ||
+        (P.temp && (!disjoint(packed, P.packed, temp, P.temp) || !disjoint(output, nout, temp, P.temp))))
+        return bad_arg("pg_wavelet_ifwt_2d_border: packed, output and temp must be distinct arrays");
+    DeviceExec ex{(cudaStream_t)stream};
+    return wv::run_ifwt_2d(ex, Fx, Fy, P, packed, output, temp);
+}
+
+int pg_wavelet_div_coeff_2d_border(int wavelet_x, int wavelet_y, const double* vx, const double* vy, int64_t h,
+                                   int64_t w, int levels, double* div, double* n, void* stream) {
+    WFilter Fx, Fy;
+    wv::Plan2d P;
+    if (!filter_of(wavelet_x, &Fx) || !filter_of(wavelet_y, &Fy))
+        return bad_arg("pg_wavelet_div_coeff_2d_border: unknown wavelet");
+    if (!wv::plan_2d(Fx, Fy, h, w, levels, &P))
+        return bad_arg("pg_wavelet_div_coeff_2d_border: h and w must be >= 2, levels in 0..40");
+    const i64 m = P.packed;
+    if (!vx || !vy || !div || !n || !disjoint(div, m, n, m) || !disjoint(div, m, vx, m) || !disjoint(div, m, vy, m) ||
+        !disjoint(n, m, vx, m) || !disjoint(n, m, vy, m))
+        return bad_arg("pg_wavelet_div_coeff_2d_border: outputs must not overlap each other or the inputs");
+    DeviceExec ex{(cudaStream_t)stream};
+    return wv::run_div_coeff_2d(ex, P, vx, vy, div, n);
 }
 
 }  // extern "C"
